@@ -1,0 +1,188 @@
+// Device numerics shared by the fit and predict kernels.
+//
+// Every floating-point step that decides a split is written with explicit
+// round-to-nearest intrinsics (no contraction, fixed order) so that the gains
+// are bit-identical to a host computation that performs the same operations
+// one at a time.  The recipes:
+//   * Philox4x32-10 counter-based RNG (Salmon, Moraes, Dror, Shaw, SC'11)
+//   * entropy gain (bits) of a 2 x C table, restating lib_ensembles/source/
+//     gpudte.cu:70-117, evaluated as float-float sums of an n*ln(n) table
+//   * variance gain nL*nR*(mL-mR)^2/(nL+nR) (lib_ensembles/source/gpuert.cu:
+//     363-378) from exact 64-bit fixed-point target sums, in float-float
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+namespace dml {
+
+// ------------------------------------------------------------------ Philox
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2,
+                                            uint32_t c3, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint32_t h0 = __umulhi(0xD2511F53u, c0), l0 = 0xD2511F53u * c0;
+    uint32_t h1 = __umulhi(0xCD9E8D57u, c2), l1 = 0xCD9E8D57u * c2;
+    uint32_t n0 = h1 ^ c1 ^ k0;
+    uint32_t n2 = h0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = l1;
+    c2 = n2;
+    c3 = l0;
+  }
+  return U4{c0, c1, c2, c3};
+}
+
+enum : uint32_t { kTagFeature = 1, kTagSample = 2, kTagBoot = 3 };
+
+// Draw keys: counter = {a, b, tree, tag<<24 | depth}, key = seed.
+__device__ __forceinline__ U4 keyed(uint64_t seed, uint32_t tag, uint32_t depth,
+                                    uint32_t tree, uint32_t a, uint32_t b) {
+  return philox4x32_10(a, b, tree, (tag << 24) | (depth & 0xFFFFFFu), (uint32_t)seed,
+                       (uint32_t)(seed >> 32));
+}
+
+__device__ __forceinline__ uint32_t pick(const U4& v, int i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// ----------------------------------------------------------- float helpers
+__device__ __forceinline__ uint32_t orderable(float x) {
+  uint32_t u = __float_as_uint(x);
+  if ((u << 1) == 0) u = 0;  // -0 and +0 are one value
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float from_orderable(uint32_t k) {
+  uint32_t u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+  return __uint_as_float(u);
+}
+__device__ __forceinline__ bool goes_left(float x, float thr) {
+  return x == -FLT_MAX || x < thr;
+}
+// Threshold between two sorted distinct values a < b: their midpoint, or b
+// where the midpoint rounds onto a (or overflows), so that {x < thr} is
+// exactly the set of values <= a.
+__device__ __forceinline__ float midpoint_threshold(float a, float b) {
+  float m = __fdiv_rn(__fadd_rn(a, b), 2.0f);
+  return (a < m && m <= b) ? m : b;
+}
+
+// ------------------------------------------------------------ float-float
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return ff{s, e};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  float s = __fadd_rn(a.hi, b.hi);
+  float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s, e);
+}
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff{-b.hi, -b.lo}); }
+__device__ __forceinline__ ff ff_from_i64(long long x) {
+  float hi = __ll2float_rn(x);
+  long long r = x - __float2ll_rz(hi);
+  return ff{hi, __ll2float_rn(r)};
+}
+__device__ __forceinline__ ff ff_div_f(ff a, float b) {
+  float q1 = __fdiv_rn(a.hi, b);
+  float p = __fmul_rn(q1, b);
+  float pe = __fmaf_rn(q1, b, -p);
+  ff r = ff_add(a, ff{-p, -pe});
+  float q2 = __fdiv_rn(r.hi, b);
+  return fast_two_sum(q1, q2);
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  float p = __fmul_rn(a.hi, b.hi);
+  float pe = __fmaf_rn(a.hi, b.hi, -p);
+  float t1 = __fmul_rn(a.hi, b.lo);
+  float t2 = __fmul_rn(a.lo, b.hi);
+  pe = __fadd_rn(pe, __fadd_rn(t1, t2));
+  return fast_two_sum(p, pe);
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+  float p = __fmul_rn(a.hi, b);
+  float pe = __fmaf_rn(a.hi, b, -p);
+  pe = __fadd_rn(pe, __fmul_rn(a.lo, b));
+  return fast_two_sum(p, pe);
+}
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(e + 127) << 23); }
+__device__ __forceinline__ float scale_pow2(float g, int e) {
+  while (e < -126) {
+    g = __fmul_rn(g, pow2f(-126));
+    e += 126;
+  }
+  while (e > 127) {
+    g = __fmul_rn(g, pow2f(127));
+    e -= 127;
+  }
+  return __fmul_rn(g, pow2f(e));
+}
+__device__ __forceinline__ double pow2d(int e) {
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+constexpr float kLn2f = 0.693147182464599609375f;
+constexpr float kSensible = 0.001f;  // gain > 1e-3 (double) <=> gain >= 0.001f
+
+__device__ __forceinline__ ff ld_ff(const float2* H, long long n) {
+  float2 v = __ldg(H + n);
+  return ff{v.x, v.y};
+}
+
+// Prior numerator h(n) - sum_c h(N_c) of a node.
+template <class CountFn>
+__device__ __forceinline__ ff entropy_prior(const float2* H, long long n, int C, CountFn cnt) {
+  ff P = ld_ff(H, n);
+  for (int c = 0; c < C; ++c) P = ff_sub(P, ld_ff(H, cnt(c)));
+  return P;
+}
+
+// Entropy gain in bits of the split with left class counts L(c), node counts
+// Ntot(c): (prior - posterior) exactly as the oracle orders it.
+template <class LeftFn, class TotFn>
+__device__ __forceinline__ float entropy_gain(const float2* H, ff P, int C, long long nL,
+                                              long long nR, LeftFn L, TotFn Ntot) {
+  ff Q{0.0f, 0.0f};
+  Q = ff_add(Q, ld_ff(H, nL));
+  for (int c = 0; c < C; ++c) Q = ff_sub(Q, ld_ff(H, L(c)));
+  Q = ff_add(Q, ld_ff(H, nR));
+  for (int c = 0; c < C; ++c) Q = ff_sub(Q, ld_ff(H, Ntot(c) - L(c)));
+  ff D = ff_sub(P, Q);
+  float den = __fmul_rn(__ll2float_rn(nL + nR), kLn2f);
+  return __fdiv_rn(D.hi, den);
+}
+
+__device__ __forceinline__ float variance_gain(long long nL, long long SL, long long nR,
+                                               long long SR, int S) {
+  ff mL = ff_div_f(ff_from_i64(SL), __ll2float_rn(nL));
+  ff mR = ff_div_f(ff_from_i64(SR), __ll2float_rn(nR));
+  ff d = ff_sub(mL, mR);
+  ff d2 = ff_mul(d, d);
+  float w = __fdiv_rn(__fmul_rn(__ll2float_rn(nL), __ll2float_rn(nR)), __ll2float_rn(nL + nR));
+  float g = ff_mul_f(d2, w).hi;
+  return scale_pow2(g, -2 * S);
+}
+
+// Candidate order: valid first, then higher gain, lower feature, lower threshold.
+__device__ __forceinline__ bool cand_better(bool va, float ga, int fa, float ta, bool vb,
+                                            float gb, int fb, float tb) {
+  if (va != vb) return va;
+  if (ga != gb) return ga > gb;
+  if (fa != fb) return fa < fb;
+  return ta < tb;
+}
+
+}  // namespace dml

@@ -1,0 +1,67 @@
+// Internal structures shared by the fit/predict host drivers and kernels.
+#pragma once
+#include <cstdint>
+
+namespace dml {
+
+constexpr int kMaxClasses = 32;
+constexpr int kMaxTries = 64;  // mandatory + optional tries evaluated per node
+
+// One forest of a fit batch (device-visible copy).
+struct ProbDesc {
+  const float* X;          // feature-major [F * N]
+  const int32_t* lab;      // classification labels [N]
+  const long long* q;      // regression targets, fixed point 2^-S [N]
+  long long N;
+  int F, C, K, n_mand, n_opt;
+  int max_depth, min_node_size, min_leaf;
+  int algo, task, S;
+  unsigned long long seed;
+  int n_trees;
+  int tree0;               // global index of tree 0 of this forest in the batch
+  long long ent0;          // entry slot of tree 0; tree t owns [ent0 + t*N, +N)
+};
+
+// An open node of the current level.  Levels are stored forest-major,
+// tree-major, parent-ordered (left before right).
+struct LNode {
+  int prob, tree, idx, depth;
+  int tstart, fstart, fend, ecnt;  // level positions: tree's / forest's first node, forest end
+  long long ebeg;                  // first entry slot
+  int n, pad;                      // weighted row count
+  long long sum;                   // regression: sum of q * w
+};
+
+// Result of a node's search + split.
+struct NodeRes {
+  int split, f;
+  float thr, gain;
+  int nl_e, nl;      // entries / weighted rows going left
+  long long suml;    // regression: left sum of q * w
+};
+
+// Node of the reference's model layout (gpudte_algorithm_shared.h:82-90).
+struct ClassifyNode {
+  int child_start, child_count, probability_start, attribute;
+  float split_point;
+};
+static_assert(sizeof(ClassifyNode) == 20, "Classify node is 20 bytes");
+
+// Predict layout: one 16-byte load per node.  Internal: {child_start,
+// attribute, split bits, 0}; leaf: {-1, voted class, value bits, 0}.
+struct PNode {
+  int a, b;
+  float t;
+  int pad;
+};
+
+// Per-level, per-forest segment of the level list (for the final gather).
+struct Seg {
+  long long node_pos;   // position in the node log
+  int node_cnt;
+  int pad;
+  long long leaf_rank;  // first leaf rank in the probability log
+  long long leaf_cnt;
+};
+
+}  // namespace dml

@@ -1,0 +1,54 @@
+// Host-side engine internals shared by the fit driver, predict and server.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/dml.h"
+#include "dml_internal.h"
+
+struct dml_forest {
+  int task = 0, n_trees = 0, n_classes = 1, n_features = 0;
+  dml::ClassifyNode* nodes = nullptr;  // device, reference layout
+  long long n_nodes = 0;
+  float* probs = nullptr;              // device
+  long long n_probs = 0;
+  dml::PNode* pnodes = nullptr;        // device, predict layout
+  int max_depth = 0;
+  double fit_ms = 0.0;
+  int device = 0;
+};
+
+namespace dml {
+
+void set_error(const char* fmt, ...);
+
+struct CudaError {
+  cudaError_t e;
+};
+
+#define DML_CK(call)                                                                    \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      ::dml::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+      throw ::dml::CudaError{e_};                                                       \
+    }                                                                                   \
+  } while (0)
+
+struct InvalidArg {};
+
+// n*ln(n) table recipe (host, IEEE double, fixed order) -> float pairs.
+void build_nlogn_table(long long nmax, float2* out);
+// Fixed-point scale of regression targets from max |y| and the row count.
+int quant_scale_from_max(float maxabs, long long n);
+
+dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s);
+
+// Stream-ordered device allocations from the device's memory pool.
+void* dev_alloc(size_t bytes, cudaStream_t s);
+void dev_free(void* p, cudaStream_t s);
+
+}  // namespace dml

@@ -1,0 +1,714 @@
+// Fit driver: the level-wise build of all trees of all forests of a batch.
+//
+// Replaces GpuDteAlgorithm<T>::Fit (lib_ensembles/source/gpudte_algorithm.cc:
+// 15-267).  Where the reference launches find-split / perform-split per chunk
+// of <= 512 nodes with four host syncs per chunk and streams level overflow
+// through host memory, this driver keeps every level on the device and issues
+// one launch set per level for every open node of every tree of every forest,
+// with one small summary read per level.  dml_fit_plain keeps the reference's
+// chunked launch structure on the same kernels.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "engine.h"
+#include "level_kernels.cuh"
+
+namespace dml {
+
+namespace {
+thread_local std::string g_last_error;
+thread_local dml_fit_stats g_last_stats;
+}  // namespace
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+const char* last_error_str() { return g_last_error.c_str(); }
+void clear_error() { g_last_error.clear(); }
+
+// ------------------------------------------------------------ host numerics
+// Same recipe as the oracle's table: ln(x) = 2*atanh((m-1)/(m+1)) + e*ln2
+// with x = m*2^e, m in [sqrt(1/2), sqrt(2)); compiled with
+// -ffp-contract=off so every operation rounds separately.
+static double table_ln(double x) {
+  int e = 0;
+  double m = std::frexp(x, &e);
+  if (m < 0.70710678118654752440) {
+    m = m * 2.0;
+    e = e - 1;
+  }
+  double z = (m - 1.0) / (m + 1.0);
+  double z2 = z * z;
+  double term = z;
+  double sum = 0.0;
+  for (int k = 0; k < 13; ++k) {
+    sum = sum + term / (double)(2 * k + 1);
+    term = term * z2;
+  }
+  return 2.0 * sum + (double)e * 0.6931471805599453094;
+}
+
+void build_nlogn_table(long long nmax, float2* out) {
+  for (long long n = 0; n <= nmax; ++n) {
+    if (n < 2) {
+      out[n] = make_float2(0.0f, 0.0f);
+      continue;
+    }
+    double h = (double)n * table_ln((double)n);
+    float hi = (float)h;
+    float lo = (float)(h - (double)hi);
+    out[n] = make_float2(hi, lo);
+  }
+}
+
+int quant_scale_from_max(float mx, long long n) {
+  if (mx == 0.0f) return 0;
+  int ey = std::ilogb(mx) + 1;
+  int en = 0;
+  while (((long long)1 << en) < n) ++en;
+  int S = 61 - ey - en;
+  if (S > 62) S = 62;
+  if (S < -60) S = -60;
+  return S;
+}
+
+void* dev_alloc(size_t bytes, cudaStream_t s) {
+  if (bytes == 0) bytes = 16;
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, s);
+  if (e != cudaSuccess) {
+    set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    cudaGetLastError();
+    throw CudaError{e};
+  }
+  return p;
+}
+void dev_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+// Keeps freed pool memory cached in this process so that repeated fits and
+// predictions reuse device buffers instead of returning to the driver.
+void init_pool_once() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  });
+}
+
+// A device buffer that grows (contents preserved) on the stream.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  void reserve(size_t n, cudaStream_t s, bool keep = true) {
+    if (n <= cap) return;
+    size_t nc = std::max(n, cap + cap / 2);
+    T* q = (T*)dev_alloc(nc * sizeof(T), s);
+    if (keep && p && cap)
+      DML_CK(cudaMemcpyAsync(q, p, cap * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    dev_free(p, s);
+    p = q;
+    cap = nc;
+  }
+  void release(cudaStream_t s) {
+    dev_free(p, s);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+constexpr int kBlock = 256;
+constexpr int kSmemCap = 4096;    // RF nodes up to this many entries sort in shared memory
+constexpr int kPlainChunk = 512;  // reference: max_blocks_ / max_nominal_ nodes per launch
+
+// n*ln(n) table cached on the device across fits (grow-only).
+struct TableCache {
+  float2* H = nullptr;
+  long long n = -1;
+  std::mutex mu;
+};
+static TableCache g_table;
+
+static const float2* nlogn_table(long long nmax, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_table.mu);
+  if (g_table.n >= nmax) return g_table.H;
+  long long n = std::max(nmax, (long long)1024);
+  std::vector<float2> h((size_t)n + 1);
+  build_nlogn_table(n, h.data());
+  float2* d = nullptr;
+  DML_CK(cudaMalloc(&d, sizeof(float2) * (n + 1)));
+  DML_CK(cudaMemcpyAsync(d, h.data(), sizeof(float2) * (n + 1), cudaMemcpyHostToDevice, s));
+  DML_CK(cudaStreamSynchronize(s));
+  if (g_table.H) cudaFree(g_table.H);
+  g_table.H = d;
+  g_table.n = n;
+  return d;
+}
+
+template <int CW>
+static void set_smem_attrs() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_rf_cta<kBlock, CW, kSmemCap>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemCap * 24);
+  });
+}
+
+template <int CW>
+static void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s) {
+  LevelArgs b = a;
+  b.nwork = count;
+  if (q == kQWarp) {
+    int blocks = std::max(1, std::min((count + 7) / 8, 1 << 20));
+    k_warp_nodes<CW><<<blocks, 256, 0, s>>>(b);
+  } else if (q == kQErt) {
+    k_ert_cta<kBlock><<<std::min(count, 1 << 20), kBlock, 0, s>>>(b);
+  } else {
+    set_smem_attrs<CW>();
+    size_t dsm = q == kQRfSmall ? (size_t)kSmemCap * 24 : 0;
+    k_rf_cta<kBlock, CW, kSmemCap><<<std::min(count, 1 << 20), kBlock, dsm, s>>>(
+        b, q == kQRfBig ? 1 : 0);
+  }
+  DML_CK(cudaGetLastError());
+}
+
+static void launch_search(int CW, int q, const LevelArgs& a, int count, cudaStream_t s) {
+  switch (CW) {
+    case 1: launch_search_cw<1>(q, a, count, s); break;
+    case 2: launch_search_cw<2>(q, a, count, s); break;
+    case 4: launch_search_cw<4>(q, a, count, s); break;
+    case 8: launch_search_cw<8>(q, a, count, s); break;
+    default: launch_search_cw<16>(q, a, count, s); break;
+  }
+}
+
+struct Summary {
+  int children, leaves;
+  int qcount[kNumQ];
+};
+
+struct ProbHost {
+  const float* X = nullptr;  // device
+  const float* y = nullptr;  // device
+  int* lab = nullptr;
+  long long* q = nullptr;
+};
+
+static void finish_stats(dml_fit_stats& st) { g_last_stats = st; }
+
+static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bool plain,
+                                        cudaStream_t s) {
+  init_pool_once();
+  // ------------------------------------------------------------ checks
+  std::vector<ProbDesc> hp(nprob);
+  std::vector<ProbHost> ph(nprob);
+  int Cmax = 1;
+  long long total_slots = 0;
+  int total_trees = 0;
+  bool any_weights = false;
+  long long H_n = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const dml_fit_desc& d = descs[i];
+    if (d.algo != DML_ALGO_RF && d.algo != DML_ALGO_ERT) {
+      set_error("forest %d: algo must be RF (0) or ERT (1)", i);
+      throw InvalidArg{};
+    }
+    if (d.task != DML_CLASSIFICATION && d.task != DML_REGRESSION) {
+      set_error("forest %d: task must be classification (0) or regression (1)", i);
+      throw InvalidArg{};
+    }
+    if (d.n_trees <= 0 || d.n_rows <= 0 || d.n_features <= 0 || !d.samples || !d.targets) {
+      set_error("forest %d: n_trees, n_rows and n_features must be positive, data non-null", i);
+      throw InvalidArg{};
+    }
+    if (d.n_rows >= (1ll << 30) || (long long)d.n_rows * d.n_features >= (1ll << 40)) {
+      set_error("forest %d: too many rows", i);
+      throw InvalidArg{};
+    }
+    if (d.task == DML_CLASSIFICATION && (d.n_classes < 1 || d.n_classes > kMaxClasses)) {
+      set_error("forest %d: n_classes must be in [1, %d]", i, kMaxClasses);
+      throw InvalidArg{};
+    }
+    if (d.max_depth < 0 || d.min_node_size < 0 || d.n_features_try < 0 ||
+        (d.memory != DML_HOST && d.memory != DML_DEVICE)) {
+      set_error("forest %d: max_depth, min_node_size, n_features_try must be >= 0", i);
+      throw InvalidArg{};
+    }
+    ProbDesc& P = hp[i];
+    std::memset(&P, 0, sizeof(P));
+    P.N = d.n_rows;
+    P.F = d.n_features;
+    P.C = d.task == DML_CLASSIFICATION ? d.n_classes : 1;
+    // kNrFeatures = 0 -> round(ln F) + 1 (gpudte_algorithm.cc:579-580)
+    P.K = d.n_features_try > 0 ? d.n_features_try
+                               : (int)std::round(std::log((double)d.n_features)) + 1;
+    // try loop bounds (gpuert.cu:144-149): K mandatory tries (F if K > F), then
+    // up to min(F - K, 10) more while the best gain stays <= 1e-3
+    P.n_mand = std::min(P.K, P.F);
+    P.n_opt = P.K < P.F ? std::min(P.F - P.K, 10) : 0;
+    if (P.n_mand + P.n_opt > kMaxTries) {
+      set_error("forest %d: at most %d tries per node", i, kMaxTries);
+      throw InvalidArg{};
+    }
+    P.max_depth = d.max_depth;
+    P.min_node_size = d.min_node_size;
+    P.min_leaf = std::max(1, d.min_leaf);
+    P.algo = d.algo;
+    P.task = d.task;
+    P.seed = d.seed;
+    P.n_trees = d.n_trees;
+    P.tree0 = total_trees;
+    P.ent0 = total_slots;
+    total_trees += d.n_trees;
+    total_slots += (long long)d.n_trees * d.n_rows;
+    Cmax = std::max(Cmax, P.C);
+    if (d.algo == DML_ALGO_RF) any_weights = true;
+    if (d.task == DML_CLASSIFICATION) H_n = std::max(H_n, (long long)d.n_rows);
+  }
+  const int CW = Cmax <= 2 ? 1 : Cmax <= 4 ? 2 : Cmax <= 8 ? 4 : Cmax <= 16 ? 8 : 16;
+  dml_fit_stats st;
+  std::memset(&st, 0, sizeof(st));
+
+  std::vector<void*> owned;
+  auto alloc = [&](size_t bytes) {
+    void* p = dev_alloc(bytes, s);
+    owned.push_back(p);
+    return p;
+  };
+  DBuf<LNode> cur, nxt;
+  DBuf<int> cnt_cur, cnt_nxt, res_cnt, childpos, leafpos;
+  DBuf<NodeRes> res_cur, res_nxt;
+  DBuf<int2> parts;
+  DBuf<int> qlist[kNumQ];
+  DBuf<ClassifyNode> node_log;
+  DBuf<float> prob_log;
+  DBuf<Seg> segs;
+  std::vector<dml_forest*> forests;
+  auto release_all = [&]() {
+    for (void* p : owned) dev_free(p, s);
+    owned.clear();
+    cur.release(s);
+    nxt.release(s);
+    cnt_cur.release(s);
+    cnt_nxt.release(s);
+    res_cnt.release(s);
+    childpos.release(s);
+    leafpos.release(s);
+    res_cur.release(s);
+    res_nxt.release(s);
+    parts.release(s);
+    for (auto& q : qlist) q.release(s);
+    node_log.release(s);
+    prob_log.release(s);
+    segs.release(s);
+  };
+  try {
+    // ---------------------------------------------------- data to device
+    int* d_err = (int*)alloc(sizeof(int) * 4);
+    unsigned* d_max = (unsigned*)alloc(sizeof(unsigned) * nprob);
+    DML_CK(cudaMemsetAsync(d_err, 0, sizeof(int) * 4, s));
+    DML_CK(cudaMemsetAsync(d_max, 0, sizeof(unsigned) * nprob, s));
+    for (int i = 0; i < nprob; ++i) {
+      const dml_fit_desc& d = descs[i];
+      ProbDesc& P = hp[i];
+      ProbHost& H = ph[i];
+      H.X = d.samples;
+      H.y = d.targets;
+      if (d.memory == DML_HOST) {
+        float* dx = (float*)alloc(sizeof(float) * P.N * P.F);
+        float* dy = (float*)alloc(sizeof(float) * P.N);
+        DML_CK(cudaMemcpyAsync(dx, d.samples, sizeof(float) * P.N * P.F, cudaMemcpyHostToDevice, s));
+        DML_CK(cudaMemcpyAsync(dy, d.targets, sizeof(float) * P.N, cudaMemcpyHostToDevice, s));
+        H.X = dx;
+        H.y = dy;
+      }
+      P.X = H.X;
+      long long nx = P.N * P.F;
+      int grid = (int)std::min<long long>(4096, (nx + 255) / 256);
+      k_validate<<<grid, 256, 0, s>>>(H.X, nx, H.y, P.N, P.task, P.C, d_err, d_max + i);
+      DML_CK(cudaGetLastError());
+      if (P.task == 0)
+        H.lab = (int*)alloc(sizeof(int) * P.N);
+      else
+        H.q = (long long*)alloc(sizeof(long long) * P.N);
+      P.lab = H.lab;
+      P.q = H.q;
+    }
+    int h_err[4] = {0, 0, 0, 0};
+    std::vector<unsigned> h_max(nprob);
+    DML_CK(cudaMemcpyAsync(h_err, d_err, sizeof(h_err), cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaMemcpyAsync(h_max.data(), d_max, sizeof(unsigned) * nprob,
+                           cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaStreamSynchronize(s));
+    if (h_err[0] & 1) {
+      set_error("samples hold NaN or infinite values (the missing-value marker is -FLT_MAX)");
+      throw InvalidArg{};
+    }
+    if (h_err[0] & 2) {
+      set_error("classification targets must be integers in [0, n_classes)");
+      throw InvalidArg{};
+    }
+    if (h_err[0] & 4) {
+      set_error("regression targets hold NaN or infinite values");
+      throw InvalidArg{};
+    }
+    for (int i = 0; i < nprob; ++i) {
+      ProbDesc& P = hp[i];
+      float mx;
+      std::memcpy(&mx, &h_max[i], 4);
+      P.S = P.task == 1 ? quant_scale_from_max(mx, P.N) : 0;
+      int grid = (int)std::min<long long>(4096, (P.N + 255) / 256);
+      k_prep_targets<<<grid, 256, 0, s>>>(ph[i].y, P.N, P.task, P.S, ph[i].lab, ph[i].q);
+      DML_CK(cudaGetLastError());
+    }
+    const float2* H = H_n > 0 ? nlogn_table(H_n, s) : nullptr;
+
+    // --------------------------------------------------------- entries
+    int* rowsA = (int*)alloc(sizeof(int) * total_slots);
+    int* rowsB = (int*)alloc(sizeof(int) * total_slots);
+    int* wA = any_weights ? (int*)alloc(sizeof(int) * total_slots) : nullptr;
+    int* wB = any_weights ? (int*)alloc(sizeof(int) * total_slots) : nullptr;
+    uint2* scratch = any_weights ? (uint2*)alloc(sizeof(uint2) * 2 * total_slots) : nullptr;
+    ProbDesc* d_probs = (ProbDesc*)alloc(sizeof(ProbDesc) * nprob);
+    DML_CK(cudaMemcpyAsync(d_probs, hp.data(), sizeof(ProbDesc) * nprob, cudaMemcpyHostToDevice, s));
+    std::vector<int> tree_prob(total_trees);
+    for (int i = 0; i < nprob; ++i)
+      for (int t = 0; t < hp[i].n_trees; ++t) tree_prob[hp[i].tree0 + t] = i;
+    int* d_tree_prob = (int*)alloc(sizeof(int) * total_trees);
+    DML_CK(cudaMemcpyAsync(d_tree_prob, tree_prob.data(), sizeof(int) * total_trees,
+                           cudaMemcpyHostToDevice, s));
+    long long* fbase[2];
+    long long* lbase[2];
+    for (int b = 0; b < 2; ++b) {
+      fbase[b] = (long long*)alloc(sizeof(long long) * nprob);
+      lbase[b] = (long long*)alloc(sizeof(long long) * nprob);
+      DML_CK(cudaMemsetAsync(fbase[b], 0, sizeof(long long) * nprob, s));
+      DML_CK(cudaMemsetAsync(lbase[b], 0, sizeof(long long) * nprob, s));
+    }
+    int* d_qcount = (int*)alloc(sizeof(int) * kNumQ);
+    int* d_summary = (int*)alloc(sizeof(int) * 2);
+    long long* d_stats = (long long*)alloc(sizeof(long long) * 2);
+    DML_CK(cudaMemsetAsync(d_stats, 0, sizeof(long long) * 2, s));
+    Summary* h_sum = nullptr;
+    DML_CK(cudaMallocHost(&h_sum, sizeof(Summary)));
+
+    cudaEvent_t ev0, ev1;
+    DML_CK(cudaEventCreate(&ev0));
+    DML_CK(cudaEventCreate(&ev1));
+    DML_CK(cudaEventRecord(ev0, s));
+
+    // ------------------------------------------------------------ roots
+    int n = total_trees;
+    cur.reserve(n, s, false);
+    cnt_cur.reserve((size_t)n * Cmax, s, false);
+    res_cur.reserve(n, s, false);
+    for (auto& q : qlist) q.reserve(n, s, false);
+    DML_CK(cudaMemsetAsync(d_qcount, 0, sizeof(int) * kNumQ, s));
+    auto queues = [&]() {
+      Queues Q;
+      for (int i = 0; i < kNumQ; ++i) Q.list[i] = qlist[i].p;
+      Q.count = d_qcount;
+      Q.rf_small_cap = kSmemCap;
+      return Q;
+    };
+    if (any_weights) {
+      DML_CK(cudaMemsetAsync(scratch, 0, sizeof(int) * total_slots, s));
+      long long maxN = 0;
+      for (auto& P : hp) maxN = std::max(maxN, P.N);
+      const int chunk = 1 << 16;
+      dim3 g((unsigned)((maxN + chunk - 1) / chunk), (unsigned)total_trees);
+      k_boot_count<<<g, 256, 0, s>>>(d_probs, d_tree_prob, (int*)scratch, chunk);
+      DML_CK(cudaGetLastError());
+      ++st.launches;
+    }
+    k_roots<1024><<<total_trees, 1024, 0, s>>>(d_probs, d_tree_prob, (const int*)scratch, rowsA,
+                                               wA, cur.p, cnt_cur.p, Cmax, res_cur.p, queues());
+    DML_CK(cudaGetLastError());
+    ++st.launches;
+    DML_CK(cudaMemcpyAsync(h_sum->qcount, d_qcount, sizeof(int) * kNumQ, cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaStreamSynchronize(s));
+
+    long long log_base = 0, plog_base = 0;
+    int depth = 0;
+    float search_ms_total = 0.0f;
+    cudaEvent_t es0, es1;
+    DML_CK(cudaEventCreate(&es0));
+    DML_CK(cudaEventCreate(&es1));
+    while (n > 0) {
+      // ------------------------------------------- search + partition
+      LevelArgs a;
+      a.probs = d_probs;
+      a.nodes = cur.p;
+      a.cnt = cnt_cur.p;
+      a.Cmax = Cmax;
+      a.res = res_cur.p;
+      res_cnt.reserve((size_t)n * Cmax, s, false);
+      a.res_cnt = res_cnt.p;
+      a.rowsA = rowsA;
+      a.wA = wA;
+      a.rowsB = rowsB;
+      a.wB = wB;
+      a.scratch = scratch;
+      a.scratch_half = total_slots;
+      a.H = H;
+      int qc[kNumQ];
+      std::memcpy(qc, h_sum->qcount, sizeof(qc));
+      DML_CK(cudaEventRecord(es0, s));
+      for (int q = 0; q < kNumQ; ++q) {
+        if (qc[q] <= 0) continue;
+        if (!plain) {
+          a.work = qlist[q].p;
+          launch_search(CW, q, a, qc[q], s);
+          ++st.launches;
+        } else {
+          for (int off = 0; off < qc[q]; off += kPlainChunk) {
+            a.work = qlist[q].p + off;
+            launch_search(CW, q, a, std::min(kPlainChunk, qc[q] - off), s);
+            ++st.launches;
+            DML_CK(cudaStreamSynchronize(s));
+          }
+        }
+      }
+      DML_CK(cudaEventRecord(es1, s));
+      // -------------------------------------------------- scans
+      int nparts = (n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
+      parts.reserve(nparts, s, false);
+      childpos.reserve((size_t)n + 1, s, false);
+      leafpos.reserve((size_t)n + 1, s, false);
+      k_scan_part<<<nparts, kScanBlock, 0, s>>>(res_cur.p, n, parts.p);
+      k_scan_top<<<1, kScanBlock, 0, s>>>(parts.p, nparts, childpos.p, leafpos.p, n, d_summary);
+      k_scan_apply<<<nparts, kScanBlock, 0, s>>>(res_cur.p, n, parts.p, childpos.p, leafpos.p);
+      DML_CK(cudaGetLastError());
+      st.launches += 3;
+      // ------------------------------------------------ emission
+      nxt.reserve((size_t)2 * n, s, false);
+      cnt_nxt.reserve((size_t)2 * n * Cmax, s, false);
+      res_nxt.reserve((size_t)2 * n, s, false);
+      for (auto& q : qlist) q.reserve((size_t)2 * n, s, false);
+      node_log.reserve((size_t)(log_base + n), s, true);
+      prob_log.reserve((size_t)(plog_base + n) * Cmax, s, true);
+      segs.reserve((size_t)(depth + 1) * nprob, s, true);
+      DML_CK(cudaMemsetAsync(segs.p + (size_t)depth * nprob, 0, sizeof(Seg) * nprob, s));
+      DML_CK(cudaMemsetAsync(d_qcount, 0, sizeof(int) * kNumQ, s));
+      // forests without nodes at this level keep their bases
+      DML_CK(cudaMemcpyAsync(fbase[(depth + 1) & 1], fbase[depth & 1], sizeof(long long) * nprob,
+                             cudaMemcpyDeviceToDevice, s));
+      DML_CK(cudaMemcpyAsync(lbase[(depth + 1) & 1], lbase[depth & 1], sizeof(long long) * nprob,
+                             cudaMemcpyDeviceToDevice, s));
+      EmitArgs e;
+      e.probs = d_probs;
+      e.cur = cur.p;
+      e.cnt = cnt_cur.p;
+      e.res = res_cur.p;
+      e.res_cnt = res_cnt.p;
+      e.childpos = childpos.p;
+      e.leafpos = leafpos.p;
+      e.n = n;
+      e.Cmax = Cmax;
+      e.log_base = log_base;
+      e.plog_base = plog_base;
+      e.node_log = node_log.p;
+      e.prob_log = prob_log.p;
+      e.fbase_cur = fbase[depth & 1];
+      e.lbase_cur = lbase[depth & 1];
+      e.fbase_next = fbase[(depth + 1) & 1];
+      e.lbase_next = lbase[(depth + 1) & 1];
+      e.seg = segs.p + (size_t)depth * nprob;
+      e.next = nxt.p;
+      e.next_cnt = cnt_nxt.p;
+      e.next_res = res_nxt.p;
+      e.Q = queues();
+      e.stats = d_stats;
+      k_emit<<<(n + 255) / 256, 256, 0, s>>>(e);
+      DML_CK(cudaGetLastError());
+      ++st.launches;
+      DML_CK(cudaMemcpyAsync(h_sum, d_summary, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+      DML_CK(cudaMemcpyAsync(h_sum->qcount, d_qcount, sizeof(int) * kNumQ,
+                             cudaMemcpyDeviceToHost, s));
+      DML_CK(cudaStreamSynchronize(s));
+      float sm = 0.0f;
+      cudaEventElapsedTime(&sm, es0, es1);
+      search_ms_total += sm;
+      log_base += n;
+      plog_base += h_sum->leaves;
+      n = h_sum->children;
+      std::swap(cur, nxt);
+      std::swap(cnt_cur, cnt_nxt);
+      std::swap(res_cur, res_nxt);
+      std::swap(rowsA, rowsB);
+      std::swap(wA, wB);
+      ++depth;
+    }
+    DML_CK(cudaEventRecord(ev1, s));
+    DML_CK(cudaEventSynchronize(ev1));
+    float loop_ms = 0.0f;
+    cudaEventElapsedTime(&loop_ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    cudaEventDestroy(es0);
+    cudaEventDestroy(es1);
+    long long h_stats[2];
+    DML_CK(cudaMemcpy(h_stats, d_stats, sizeof(h_stats), cudaMemcpyDeviceToHost));
+    cudaFreeHost(h_sum);
+    st.nodes = log_base;
+    st.entries = h_stats[0];
+    st.weighted_rows = h_stats[1];
+    st.levels = depth;
+    st.level_loop_ms = loop_ms;
+    st.search_ms = search_ms_total;
+
+    // --------------------------------------------------- per-forest models
+    std::vector<long long> fnodes(nprob), fleaves(nprob);
+    DML_CK(cudaMemcpyAsync(fnodes.data(), fbase[depth & 1], sizeof(long long) * nprob,
+                           cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaMemcpyAsync(fleaves.data(), lbase[depth & 1], sizeof(long long) * nprob,
+                           cudaMemcpyDeviceToHost, s));
+    std::vector<Seg> hseg((size_t)depth * nprob);
+    if (nprob > 1 && depth > 0)
+      DML_CK(cudaMemcpyAsync(hseg.data(), segs.p, sizeof(Seg) * hseg.size(),
+                             cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < nprob; ++i) {
+      dml_forest* f = new dml_forest();
+      forests.push_back(f);
+      f->task = hp[i].task;
+      f->n_trees = hp[i].n_trees;
+      f->n_classes = hp[i].C;
+      f->n_features = hp[i].F;
+      f->n_nodes = fnodes[i];
+      f->n_probs = fleaves[i] * hp[i].C;
+      f->fit_ms = loop_ms;
+      cudaGetDevice(&f->device);
+      DML_CK(cudaMalloc(&f->nodes, sizeof(ClassifyNode) * std::max<long long>(1, f->n_nodes)));
+      DML_CK(cudaMalloc(&f->probs, sizeof(float) * std::max<long long>(1, f->n_probs)));
+      if (nprob == 1) {
+        DML_CK(cudaMemcpyAsync(f->nodes, node_log.p, sizeof(ClassifyNode) * f->n_nodes,
+                               cudaMemcpyDeviceToDevice, s));
+        DML_CK(cudaMemcpyAsync(f->probs, prob_log.p, sizeof(float) * f->n_probs,
+                               cudaMemcpyDeviceToDevice, s));
+        f->max_depth = depth - 1;
+      } else {
+        long long no = 0, po = 0;
+        for (int d = 0; d < depth; ++d) {
+          const Seg& sg = hseg[(size_t)d * nprob + i];
+          if (sg.node_cnt <= 0) continue;
+          f->max_depth = d;
+          k_gather_nodes<<<(sg.node_cnt + 255) / 256, 256, 0, s>>>(node_log.p, sg.node_pos,
+                                                                   sg.node_cnt, f->nodes + no);
+          no += sg.node_cnt;
+          if (sg.leaf_cnt > 0) {
+            long long tot = sg.leaf_cnt * hp[i].C;
+            int g = (int)std::min<long long>(4096, (tot + 255) / 256);
+            k_gather_probs<<<g, 256, 0, s>>>(prob_log.p, sg.leaf_rank, sg.leaf_cnt, Cmax,
+                                             hp[i].C, f->probs + po);
+            po += tot;
+          }
+        }
+        DML_CK(cudaGetLastError());
+      }
+      dml_status ps = forest_build_pnodes(f, s);
+      if (ps != DML_OK) throw CudaError{cudaErrorUnknown};
+    }
+    DML_CK(cudaStreamSynchronize(s));
+    release_all();
+    DML_CK(cudaStreamSynchronize(s));
+    finish_stats(st);
+  } catch (...) {
+    for (dml_forest* f : forests) {
+      if (f) {
+        cudaFree(f->nodes);
+        cudaFree(f->probs);
+        cudaFree(f->pnodes);
+        delete f;
+      }
+    }
+    release_all();
+    cudaStreamSynchronize(s);
+    throw;
+  }
+  return forests;
+}
+
+dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s) {
+  cudaFree(f->pnodes);
+  f->pnodes = nullptr;
+  if (cudaMalloc(&f->pnodes, sizeof(PNode) * std::max<long long>(1, f->n_nodes)) != cudaSuccess) {
+    set_error("device allocation failed for the predict layout");
+    return DML_ERR_OOM;
+  }
+  int g = (int)std::min<long long>(8192, (f->n_nodes + 255) / 256 + 1);
+  k_to_pnodes<<<g, 256, 0, s>>>(f->nodes, f->n_nodes, f->probs, f->n_classes, f->task, f->pnodes);
+  if (cudaGetLastError() != cudaSuccess) {
+    set_error("launch failure building the predict layout");
+    return DML_ERR_CUDA;
+  }
+  return DML_OK;
+}
+
+static dml_status fit_entry(const dml_fit_desc* descs, int n, dml_forest** out, void* stream,
+                            bool plain) {
+  clear_error();
+  if (!descs || !out || n <= 0) {
+    set_error("null argument");
+    return DML_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  try {
+    std::vector<dml_forest*> fs = run_fit(descs, n, plain, s);
+    for (int i = 0; i < n; ++i) out[i] = fs[i];
+    return DML_OK;
+  } catch (InvalidArg&) {
+    return DML_ERR_INVALID_ARG;
+  } catch (CudaError& e) {
+    return e.e == cudaErrorMemoryAllocation ? DML_ERR_OOM : DML_ERR_CUDA;
+  } catch (std::bad_alloc&) {
+    set_error("host allocation failed");
+    return DML_ERR_OOM;
+  } catch (...) {
+    set_error("internal error");
+    return DML_ERR_INTERNAL;
+  }
+}
+
+}  // namespace dml
+
+extern "C" {
+
+dml_status dml_fit(const dml_fit_desc* desc, dml_forest** out, void* stream) {
+  return dml::fit_entry(desc, 1, out, stream, false);
+}
+
+dml_status dml_fit_batched(int32_t n, const dml_fit_desc* descs, dml_forest** out, void* stream) {
+  return dml::fit_entry(descs, n, out, stream, false);
+}
+
+dml_status dml_fit_plain(const dml_fit_desc* desc, dml_forest** out, void* stream) {
+  return dml::fit_entry(desc, 1, out, stream, true);
+}
+
+dml_status dml_last_fit_stats(dml_fit_stats* stats) {
+  if (!stats) return DML_ERR_INVALID_ARG;
+  *stats = dml::g_last_stats;
+  return DML_OK;
+}
+
+const char* dml_last_error(void) { return dml::last_error_str(); }
+
+}  // extern "C"

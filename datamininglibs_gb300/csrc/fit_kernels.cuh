@@ -1,0 +1,746 @@
+// Fit kernels: root construction, per-level split search + stable partition
+// (ERT and RF, classification and regression), level scans and model emission.
+//
+// Reference path restated (lib_ensembles/source):
+//   gpurf.cu:58-129 / gpuert.cu:54-118   tree-batch init (bootstrap / identity)
+//   gpuert.cu:119-247, 275-381           ERT node search
+//   gpurf.cu:131-259, 440-917            RF node search (sort + boundary scan)
+//   gpudte.cu:156-309                    node split: partition, children, leaf
+//   gpudte_algorithm.cc:46-92            level-by-level node-array assembly
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dml_device.cuh"
+#include "dml_internal.h"
+
+namespace dml {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// -------------------------------------------------------------- block scans
+template <int BLOCK, class T>
+__device__ __forceinline__ T block_excl_scan(T v, T* total, T* sm) {
+  constexpr int NW = BLOCK / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    T t = lane < NW ? sm[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(kFull, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < NW) sm[lane] = t;
+  }
+  __syncthreads();
+  T base = w ? sm[w - 1] : T(0);
+  *total = sm[NW - 1];
+  __syncthreads();
+  return base + x - v;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_excl_scan(T v) {
+  const int lane = threadIdx.x & 31;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  return x - v;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// ----------------------------------------------------------- candidates
+struct Cand {
+  int valid;
+  float gain;
+  int f;
+  float thr;
+  int nl_e, nl;
+  long long suml;
+};
+
+__device__ __forceinline__ bool better(const Cand& a, const Cand& b) {
+  return cand_better(a.valid != 0, a.gain, a.f, a.thr, b.valid != 0, b.gain, b.f, b.thr);
+}
+
+__device__ __forceinline__ int feature_of_try(const ProbDesc& P, const LNode& nd, int t) {
+  U4 w = keyed(P.seed, kTagFeature, (uint32_t)nd.depth, (uint32_t)nd.tree, (uint32_t)nd.idx,
+               (uint32_t)t);
+  return (int)(w.x % (uint32_t)P.F);
+}
+
+// ERT threshold: mean of 10 node values drawn with replacement, summed in
+// draw order in FP32 (gpuert.cu:167-183 with a fixed order).
+__device__ __forceinline__ float ert_threshold(const ProbDesc& P, const LNode& nd, int t, int f,
+                                               const int* rows) {
+  const float* xf = P.X + (long long)f * P.N;
+  float v[10];
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {
+    U4 w = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)nd.tree, (uint32_t)nd.idx,
+                 (uint32_t)(t * 3 + g));
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      int j = g * 4 + s;
+      if (j < 10) {
+        uint32_t pos = pick(w, s) % (uint32_t)nd.ecnt;
+        v[j] = __ldg(xf + __ldg(rows + pos));
+      }
+    }
+  }
+  float acc = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 10; ++j) acc = __fadd_rn(acc, v[j]);
+  return __fdiv_rn(acc, 10.0f);
+}
+
+// ------------------------------------------------------- stable partition
+// Entries [ebeg, ebeg+m) of (rowsA, wA) into (rowsB, wB): left entries first
+// in their order, then right entries in their order (gpudte.cu:205-232 made
+// stable).  wA may be null (unit weights).
+template <int BLOCK>
+__device__ void cta_partition(const int* rowsA, const int* wA, int* rowsB, int* wB,
+                              long long ebeg, int m, int nl_e, const float* xf, float thr,
+                              int* sm) {
+  int offl = 0, offr = 0;
+  for (int base = 0; base < m; base += BLOCK) {
+    int i = base + threadIdx.x;
+    int row = 0, w = 1, left = 0;
+    if (i < m) {
+      row = rowsA[ebeg + i];
+      if (wA) w = wA[ebeg + i];
+      left = goes_left(__ldg(xf + row), thr) ? 1 : 0;
+    }
+    int tot;
+    int pos = block_excl_scan<BLOCK, int>(left, &tot, sm);
+    if (i < m) {
+      long long dst = left ? ebeg + offl + pos : ebeg + nl_e + offr + (threadIdx.x - pos);
+      rowsB[dst] = row;
+      if (wB) wB[dst] = w;
+    }
+    offl += tot;
+    offr += min(BLOCK, m - base) - tot;
+  }
+}
+
+__device__ __forceinline__ void write_result(NodeRes* res, int* res_cnt, int Cmax, int node,
+                                             const Cand& b, const int* Lc, int C) {
+  NodeRes r;
+  r.split = 1;
+  r.f = b.f;
+  r.thr = b.thr;
+  r.gain = b.gain;
+  r.nl_e = b.nl_e;
+  r.nl = b.nl;
+  r.suml = b.suml;
+  res[node] = r;
+  if (Lc)
+    for (int c = 0; c < C; ++c) res_cnt[(long long)node * Cmax + c] = Lc[c];
+}
+
+__device__ __forceinline__ void write_leaf(NodeRes* res, int node) {
+  NodeRes r;
+  r.split = 0;
+  r.f = -1;
+  r.thr = 0.0f;
+  r.gain = 0.0f;
+  r.nl_e = 0;
+  r.nl = 0;
+  r.suml = 0;
+  res[node] = r;
+}
+
+struct LevelArgs {
+  const ProbDesc* probs;
+  const LNode* nodes;
+  const int* cnt;       // node class counts [node * Cmax]
+  int Cmax;
+  const int* work;      // node ids
+  int nwork;
+  NodeRes* res;
+  int* res_cnt;         // left class counts of the chosen split [node * Cmax]
+  const int* rowsA;
+  const int* wA;        // null for unit weights (ERT)
+  int* rowsB;
+  int* wB;
+  uint2* scratch;       // two pair buffers per entry slot: scratch[slot], scratch[slot + total]
+  long long scratch_half;
+  const float2* H;      // n*ln(n) table
+};
+
+// ================================================================== ERT (CTA)
+// One CTA per node: thresholds of a chunk of tries, one pass over the node's
+// entries building every try's 2 x C histogram with warp ballots, gains,
+// the try loop's decision, then the stable partition.
+constexpr int kErtChunk = 16;
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
+  constexpr int NW = BLOCK / 32;
+  __shared__ int s_f[kErtChunk];
+  __shared__ float s_thr[kErtChunk];
+  __shared__ int s_cntw[NW][kErtChunk][kMaxClasses];   // per-warp left class counts
+  __shared__ long long s_sumw[NW][kErtChunk];          // per-warp left target sums
+  __shared__ int s_nlw[NW][kErtChunk];                 // per-warp left counts (regression)
+  __shared__ Cand s_cand[kErtChunk];
+  __shared__ int s_L[kErtChunk][kMaxClasses];
+  __shared__ int s_bestL[kMaxClasses];
+  __shared__ Cand s_best;
+  __shared__ int s_phase;  // 0 stop, 1 run optional chunk
+  __shared__ int s_scan[NW];
+  __shared__ ff s_prior;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int wi = blockIdx.x; wi < a.nwork; wi += gridDim.x) {
+    const int node = a.work[wi];
+    const LNode nd = a.nodes[node];
+    const ProbDesc& P = a.probs[nd.prob];
+    const int C = P.C;
+    const int* rows = a.rowsA + nd.ebeg;
+    const int* ncnt = a.cnt + (long long)node * a.Cmax;
+    const int ml = max(1, P.min_leaf);
+    if (threadIdx.x == 0 && P.task == 0)
+      s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
+    // chunks: mandatory tries [0, n_mand) in chunks, then one optional chunk
+    int t0 = 0;
+    bool optional = false;
+    while (true) {
+      const int tcount = optional ? P.n_opt : min(kErtChunk, P.n_mand - t0);
+      if (threadIdx.x < tcount) {
+        int t = t0 + threadIdx.x;
+        int f = feature_of_try(P, nd, t);
+        s_f[threadIdx.x] = f;
+        s_thr[threadIdx.x] = ert_threshold(P, nd, t, f, rows);
+      }
+      for (int i = threadIdx.x; i < NW * kErtChunk * kMaxClasses; i += BLOCK)
+        (&s_cntw[0][0][0])[i] = 0;
+      for (int i = threadIdx.x; i < NW * kErtChunk; i += BLOCK) {
+        (&s_sumw[0][0])[i] = 0;
+        (&s_nlw[0][0])[i] = 0;
+      }
+      __syncthreads();
+      // one pass over the entries
+      for (int base = warp * 32; base < nd.ecnt; base += BLOCK) {
+        const int i = base + lane;
+        const bool valid = i < nd.ecnt;
+        const int row = valid ? __ldg(rows + i) : 0;
+        if (P.task == 0) {
+          const int k = valid ? __ldg(P.lab + row) : -1;
+          unsigned my = 0;
+          for (int c = 0; c < C; ++c) {
+            unsigned mc = __ballot_sync(kFull, k == c);
+            if (lane == c) my = mc;
+          }
+          for (int t = 0; t < tcount; ++t) {
+            bool left = valid && goes_left(__ldg(P.X + (long long)s_f[t] * P.N + row), s_thr[t]);
+            unsigned lm = __ballot_sync(kFull, left);
+            if (lane < C) s_cntw[warp][t][lane] += __popc(lm & my);
+          }
+        } else {
+          const long long qv = valid ? __ldg(P.q + row) : 0;
+          for (int t = 0; t < tcount; ++t) {
+            bool left = valid && goes_left(__ldg(P.X + (long long)s_f[t] * P.N + row), s_thr[t]);
+            unsigned lm = __ballot_sync(kFull, left);
+            long long s = warp_sum<long long>(left ? qv : 0);
+            if (lane == 0) {
+              s_nlw[warp][t] += __popc(lm);
+              s_sumw[warp][t] += s;
+            }
+          }
+        }
+      }
+      __syncthreads();
+      // reduce warps, gains per try
+      if (P.task == 0) {
+        for (int i = threadIdx.x; i < tcount * C; i += BLOCK) {
+          int t = i / C, c = i % C, s = 0;
+          for (int w = 0; w < NW; ++w) s += s_cntw[w][t][c];
+          s_L[t][c] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x < tcount) {
+          const int t = threadIdx.x;
+          long long nl = 0;
+          for (int c = 0; c < C; ++c) nl += s_L[t][c];
+          long long nr = (long long)nd.n - nl;
+          Cand cd;
+          cd.f = s_f[t];
+          cd.thr = s_thr[t];
+          cd.nl_e = (int)nl;
+          cd.nl = (int)nl;
+          cd.suml = 0;
+          cd.valid = nl >= ml && nr >= ml;
+          cd.gain = cd.valid ? entropy_gain(
+                                   a.H, s_prior, C, nl, nr,
+                                   [&](int c) { return (long long)s_L[t][c]; },
+                                   [&](int c) { return (long long)ncnt[c]; })
+                             : -FLT_MAX;
+          s_cand[t] = cd;
+        }
+      } else {
+        if (threadIdx.x < tcount) {
+          const int t = threadIdx.x;
+          long long nl = 0, sl = 0;
+          for (int w = 0; w < NW; ++w) {
+            nl += s_nlw[w][t];
+            sl += s_sumw[w][t];
+          }
+          long long nr = (long long)nd.n - nl;
+          Cand cd;
+          cd.f = s_f[t];
+          cd.thr = s_thr[t];
+          cd.nl_e = (int)nl;
+          cd.nl = (int)nl;
+          cd.suml = sl;
+          cd.valid = nl >= ml && nr >= ml;
+          cd.gain = cd.valid ? variance_gain(nl, sl, nr, nd.sum - sl, P.S) : -FLT_MAX;
+          s_cand[t] = cd;
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int next = 0;
+        if (!optional) {
+          for (int t = 0; t < tcount; ++t) {
+            if ((t0 + t == 0) || better(s_cand[t], s_best)) {
+              s_best = s_cand[t];
+              if (P.task == 0)
+                for (int c = 0; c < C; ++c) s_bestL[c] = s_L[t][c];
+            }
+          }
+          if (t0 + tcount < P.n_mand)
+            next = 1;  // more mandatory tries
+          else if (P.n_opt > 0 && !(s_best.valid && s_best.gain >= kSensible))
+            next = 2;
+        } else {
+          for (int t = 0; t < tcount; ++t) {
+            if (better(s_cand[t], s_best)) {
+              s_best = s_cand[t];
+              if (P.task == 0)
+                for (int c = 0; c < C; ++c) s_bestL[c] = s_L[t][c];
+            }
+            if (s_cand[t].valid && s_cand[t].gain >= kSensible) break;
+          }
+        }
+        s_phase = next;
+      }
+      __syncthreads();
+      const int ph = s_phase;
+      __syncthreads();
+      if (ph == 0) break;
+      if (ph == 1) t0 += tcount;
+      if (ph == 2) {
+        optional = true;
+        t0 = P.n_mand;
+      }
+    }
+    const Cand b = s_best;
+    if (!b.valid) {
+      if (threadIdx.x == 0) write_leaf(a.res, node);
+    } else {
+      if (threadIdx.x == 0)
+        write_result(a.res, a.res_cnt, a.Cmax, node, b, P.task == 0 ? s_bestL : nullptr, C);
+      cta_partition<BLOCK>(a.rowsA, a.wA, a.rowsB, a.wB, nd.ebeg, nd.ecnt, b.nl_e,
+                           P.X + (long long)b.f * P.N, b.thr, s_scan);
+    }
+    __syncthreads();
+  }
+}
+
+// ============================================================ RF (CTA, sorted)
+// Radix sort (LSD, 8-bit digits) of (key, value) pairs held in shared memory
+// or, for large nodes, in global scratch processed tile by tile.  Stability
+// comes from per-warp contiguous chunks and in-order ranking with
+// __match_any_sync.
+template <int BLOCK>
+struct SortSmem {
+  unsigned hist[BLOCK / 32][256];
+  unsigned digit_base[256];
+  unsigned scan_tmp[BLOCK / 32];
+};
+
+template <int BLOCK>
+__device__ void radix_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                           uint32_t* vout, int m, int shift, SortSmem<BLOCK>& S) {
+  constexpr int NW = BLOCK / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int chunk = ((m + NW - 1) / NW + 31) & ~31;
+  const int beg = min(m, warp * chunk), end = min(m, beg + chunk);
+  for (int i = threadIdx.x; i < NW * 256; i += BLOCK) (&S.hist[0][0])[i] = 0;
+  __syncthreads();
+  for (int i = beg + lane; i < end; i += 32) atomicAdd(&S.hist[warp][(kin[i] >> shift) & 255u], 1u);
+  __syncthreads();
+  // digit-major, warp-minor exclusive offsets
+  {
+    const int d = threadIdx.x;
+    unsigned tot = 0;
+    if (d < 256)
+      for (int w = 0; w < NW; ++w) tot += S.hist[w][d];
+    unsigned total;
+    unsigned base = block_excl_scan<BLOCK, unsigned>(d < 256 ? tot : 0u, &total, S.scan_tmp);
+    if (d < 256) {
+      unsigned run = base;
+      for (int w = 0; w < NW; ++w) {
+        unsigned h = S.hist[w][d];
+        S.hist[w][d] = run;
+        run += h;
+      }
+    }
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  for (int b = beg; b < end; b += 32) {
+    const int i = b + lane;
+    const bool act = i < end;
+    const unsigned mask = __ballot_sync(kFull, act);
+    if (act) {
+      uint32_t k = kin[i], v = vin[i];
+      unsigned d = (k >> shift) & 255u;
+      unsigned peers = __match_any_sync(mask, d);
+      unsigned pos = S.hist[warp][d] + __popc(peers & lt);
+      kout[pos] = k;
+      vout[pos] = v;
+      __syncwarp(mask);
+      if ((peers & lt) == 0) S.hist[warp][d] += __popc(peers);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+}
+
+// Sorts pairs in place (result back in k/v).  Passes whose digit is constant
+// across all keys are skipped.
+template <int BLOCK>
+__device__ void cta_radix_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2, int m,
+                               SortSmem<BLOCK>& S, unsigned* red) {
+  // OR / AND of all keys
+  unsigned o = 0, an = 0xFFFFFFFFu;
+  for (int i = threadIdx.x; i < m; i += BLOCK) {
+    o |= k[i];
+    an &= k[i];
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    o |= __shfl_xor_sync(kFull, o, s);
+    an &= __shfl_xor_sync(kFull, an, s);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[2 * (threadIdx.x >> 5)] = o;
+    red[2 * (threadIdx.x >> 5) + 1] = an;
+  }
+  __syncthreads();
+  unsigned diff = 0;
+  {
+    unsigned oo = 0, aa = 0xFFFFFFFFu;
+    for (int w = 0; w < BLOCK / 32; ++w) {
+      oo |= red[2 * w];
+      aa &= red[2 * w + 1];
+    }
+    diff = oo ^ aa;
+  }
+  __syncthreads();
+  bool in_primary = true;
+  for (int shift = 0; shift < 32; shift += 8) {
+    if (((diff >> shift) & 255u) == 0) continue;
+    if (in_primary)
+      radix_pass<BLOCK>(k, v, k2, v2, m, shift, S);
+    else
+      radix_pass<BLOCK>(k2, v2, k, v, m, shift, S);
+    in_primary = !in_primary;
+  }
+  if (!in_primary) {
+    for (int i = threadIdx.x; i < m; i += BLOCK) {
+      k[i] = k2[i];
+      v[i] = v2[i];
+    }
+    __syncthreads();
+  }
+}
+
+// Best boundary of sorted pairs: classification with packed 2 x 32-bit class
+// prefix counts (CW = ceil(C/2) words), or regression with count / sum scans.
+// Writes the try's candidate and (classification) the left class counts of
+// the chosen boundary into candL.
+template <int BLOCK, int CW>
+__device__ void cta_best_boundary(const uint32_t* sk, const uint32_t* sv, int m, const LNode& nd,
+                                  const ProbDesc& P, const int* ncnt, const int* lw_lab,
+                                  const int* lw_w, const long long* vq, const float2* H,
+                                  ff prior, Cand* cand, int* candL, int f, const float* xf,
+                                  const int* rows, unsigned long long* sm64, int* sm_bestpos,
+                                  float* sm_bestg, unsigned long long* carry) {
+  const int C = P.C;
+  const int ml = max(1, P.min_leaf);
+  float my_g = -FLT_MAX;
+  int my_p = -1;
+  unsigned long long myL[CW > 0 ? CW : 1];
+  long long my_nl = 0, my_sl = 0;
+  if (threadIdx.x < 2 * CW + 2) carry[threadIdx.x] = 0;
+  __syncthreads();
+  for (int base = 0; base < m; base += BLOCK) {
+    const int p = base + threadIdx.x;
+    const bool act = p < m;
+    const int e = act ? (int)sv[p] : 0;
+    const int w = act ? (lw_w ? lw_w[e] : 1) : 0;
+    if (P.task == 0) {
+      const int k = act ? lw_lab[e] : -1;
+      unsigned long long L[CW > 0 ? CW : 1];
+      long long nl = 0;
+#pragma unroll
+      for (int j = 0; j < CW; ++j) {
+        unsigned long long v = (k == 2 * j ? (unsigned long long)w : 0ull) |
+                               (k == 2 * j + 1 ? ((unsigned long long)w << 32) : 0ull);
+        unsigned long long tot;
+        unsigned long long ex = block_excl_scan<BLOCK, unsigned long long>(v, &tot, sm64);
+        L[j] = ex + carry[j];
+        nl += (long long)(L[j] & 0xFFFFFFFFull) + (long long)(L[j] >> 32);
+        __syncthreads();
+        if (threadIdx.x == 0) carry[j] += tot;
+      }
+      __syncthreads();
+      if (act && p > 0 && sk[p - 1] < sk[p]) {
+        long long nr = (long long)nd.n - nl;
+        if (nl >= ml && nr >= ml) {
+          float g = entropy_gain(
+              H, prior, C, nl, nr,
+              [&](int c) {
+                unsigned long long x = L[0];
+#pragma unroll
+                for (int j = 1; j < CW; ++j)
+                  if ((c >> 1) == j) x = L[j];
+                return (long long)((c & 1) ? (x >> 32) : (x & 0xFFFFFFFFull));
+              },
+              [&](int c) { return (long long)ncnt[c]; });
+          if (my_p < 0 || g > my_g) {
+            my_g = g;
+            my_p = p;
+#pragma unroll
+            for (int j = 0; j < CW; ++j) myL[j] = L[j];
+            my_nl = nl;
+          }
+        }
+      }
+    } else {
+      const long long qw = act ? vq[e] * (long long)w : 0;
+      unsigned long long totn, tots;
+      long long exn = (long long)block_excl_scan<BLOCK, unsigned long long>(
+          (unsigned long long)w, &totn, sm64);
+      long long nl = exn + (long long)carry[0];
+      long long exs = (long long)block_excl_scan<BLOCK, unsigned long long>(
+          (unsigned long long)qw, &tots, sm64);
+      long long sl = exs + (long long)carry[1];
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        carry[0] += totn;
+        carry[1] += tots;
+      }
+      __syncthreads();
+      if (act && p > 0 && sk[p - 1] < sk[p]) {
+        long long nr = (long long)nd.n - nl;
+        if (nl >= ml && nr >= ml) {
+          float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
+          if (my_p < 0 || g > my_g) {
+            my_g = g;
+            my_p = p;
+            my_nl = nl;
+            my_sl = sl;
+          }
+        }
+      }
+    }
+  }
+  // block argmax: higher gain, then lower position
+  sm_bestg[threadIdx.x] = my_g;
+  sm_bestpos[threadIdx.x] = my_p;
+  __syncthreads();
+  for (int s = BLOCK / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      float g2 = sm_bestg[threadIdx.x + s];
+      int p2 = sm_bestpos[threadIdx.x + s];
+      float g1 = sm_bestg[threadIdx.x];
+      int p1 = sm_bestpos[threadIdx.x];
+      bool take = p2 >= 0 && (p1 < 0 || g2 > g1 || (g2 == g1 && p2 < p1));
+      if (take) {
+        sm_bestg[threadIdx.x] = g2;
+        sm_bestpos[threadIdx.x] = p2;
+      }
+    }
+    __syncthreads();
+  }
+  const int bp = sm_bestpos[0];
+  if (bp >= 0 && my_p == bp) {  // the winning thread publishes its prefix
+    Cand c;
+    c.valid = 1;
+    c.gain = my_g;
+    c.f = f;
+    float xa = __ldg(xf + rows[sv[bp - 1]]);
+    float xb = __ldg(xf + rows[sv[bp]]);
+    c.thr = midpoint_threshold(xa, xb);
+    c.nl_e = bp;
+    c.nl = (int)my_nl;
+    c.suml = my_sl;
+    *cand = c;
+    if (P.task == 0)
+      for (int cc = 0; cc < C; ++cc) {
+        unsigned long long x = myL[0];
+#pragma unroll
+        for (int j = 1; j < CW; ++j)
+          if ((cc >> 1) == j) x = myL[j];
+        candL[cc] = (int)((cc & 1) ? (x >> 32) : (x & 0xFFFFFFFFull));
+      }
+  }
+  if (bp < 0 && threadIdx.x == 0) {
+    Cand c;
+    c.valid = 0;
+    c.gain = -FLT_MAX;
+    c.f = f;
+    c.thr = 0.0f;
+    c.nl_e = 0;
+    c.nl = 0;
+    c.suml = 0;
+    *cand = c;
+  }
+  __syncthreads();
+}
+
+// RF node in a CTA.  SMEM_CAP: nodes with at most that many entries are
+// sorted in shared memory; larger ones use the node's own slots of the other
+// entry buffer and the scratch buffer as tile-sorted global storage.
+template <int BLOCK, int CW, int SMEM_CAP>
+__global__ void __launch_bounds__(BLOCK) k_rf_cta(LevelArgs a, int big) {
+  __shared__ SortSmem<BLOCK> S;
+  __shared__ unsigned long long sm64[BLOCK / 32];
+  __shared__ unsigned red[2 * (BLOCK / 32)];
+  __shared__ int sm_bestpos[BLOCK];
+  __shared__ float sm_bestg[BLOCK];
+  __shared__ unsigned long long carry[2 * 16 + 2];
+  __shared__ Cand s_cand, s_best;
+  __shared__ int s_candL[kMaxClasses], s_bestL[kMaxClasses];
+  __shared__ ff s_prior;
+  __shared__ int s_scan[BLOCK / 32];
+  __shared__ int s_next;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  for (int wi = blockIdx.x; wi < a.nwork; wi += gridDim.x) {
+    const int node = a.work[wi];
+    const LNode nd = a.nodes[node];
+    const ProbDesc& P = a.probs[nd.prob];
+    const int C = P.C;
+    const int m = nd.ecnt;
+    const int* rows = a.rowsA + nd.ebeg;
+    const int* wts = a.wA ? a.wA + nd.ebeg : nullptr;
+    const int* ncnt = a.cnt + (long long)node * a.Cmax;
+    // per-entry labels / targets, keys and values
+    uint32_t *k1, *v1, *k2, *v2;
+    int* lab_e = nullptr;
+    long long* q_e = nullptr;
+    if (!big) {
+      uint32_t* base = (uint32_t*)dsm;
+      k1 = base;
+      v1 = base + SMEM_CAP;
+      k2 = base + 2 * SMEM_CAP;
+      v2 = base + 3 * SMEM_CAP;
+      if (P.task == 0)
+        lab_e = (int*)(base + 4 * SMEM_CAP);
+      else
+        q_e = (long long*)(base + 4 * SMEM_CAP);
+      for (int i = threadIdx.x; i < m; i += BLOCK) {
+        int row = __ldg(rows + i);
+        if (P.task == 0)
+          lab_e[i] = __ldg(P.lab + row);
+        else
+          q_e[i] = __ldg(P.q + row);
+      }
+    } else {
+      // pairs: (rowsB, wB) slots of the node as one uint2-sized buffer is not
+      // available separately, so the scratch holds both ping-pong buffers
+      uint2* sc = a.scratch;
+      k1 = (uint32_t*)(sc + nd.ebeg);
+      v1 = k1 + m;
+      k2 = (uint32_t*)(sc + a.scratch_half + nd.ebeg);
+      v2 = k2 + m;
+    }
+    if (threadIdx.x == 0 && P.task == 0)
+      s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
+    __syncthreads();
+    int t = 0;
+    bool stop = false;
+    while (!stop) {
+      const int f = feature_of_try(P, nd, t);
+      const float* xf = P.X + (long long)f * P.N;
+      for (int i = threadIdx.x; i < m; i += BLOCK) {
+        k1[i] = orderable(__ldg(xf + __ldg(rows + i)));
+        v1[i] = (uint32_t)i;
+      }
+      __syncthreads();
+      cta_radix_sort<BLOCK>(k1, v1, k2, v2, m, S, red);
+      // labels / targets: smem copies for small nodes, gathers for big ones
+      if (!big) {
+        cta_best_boundary<BLOCK, CW>(k1, v1, m, nd, P, ncnt, lab_e, wts, q_e, a.H, s_prior,
+                                     &s_cand, s_candL, f, xf, rows, sm64, sm_bestpos, sm_bestg,
+                                     carry);
+      } else {
+        // gather labels/targets by entry index from global memory: stage the
+        // per-entry values in the second pair buffer (no longer needed)
+        if (P.task == 0) {
+          int* le = (int*)k2;
+          for (int i = threadIdx.x; i < m; i += BLOCK) le[i] = __ldg(P.lab + __ldg(rows + i));
+          __syncthreads();
+          cta_best_boundary<BLOCK, CW>(k1, v1, m, nd, P, ncnt, le, wts, nullptr, a.H, s_prior,
+                                       &s_cand, s_candL, f, xf, rows, sm64, sm_bestpos,
+                                       sm_bestg, carry);
+        } else {
+          long long* qe = (long long*)k2;  // k2,v2 contiguous: 8 bytes per entry
+          for (int i = threadIdx.x; i < m; i += BLOCK) qe[i] = __ldg(P.q + __ldg(rows + i));
+          __syncthreads();
+          cta_best_boundary<BLOCK, CW>(k1, v1, m, nd, P, ncnt, nullptr, wts, qe, a.H, s_prior,
+                                       &s_cand, s_candL, f, xf, rows, sm64, sm_bestpos,
+                                       sm_bestg, carry);
+        }
+      }
+      if (threadIdx.x == 0) {
+        const bool mand = t < P.n_mand;
+        if (t == 0 || better(s_cand, s_best)) {
+          s_best = s_cand;
+          if (P.task == 0)
+            for (int c = 0; c < C; ++c) s_bestL[c] = s_candL[c];
+        }
+        bool next;
+        if (mand)
+          next = (t + 1 < P.n_mand) ||
+                 (P.n_opt > 0 && !(s_best.valid && s_best.gain >= kSensible));
+        else
+          next = !(s_cand.valid && s_cand.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
+        s_next = next ? 1 : 0;
+      }
+      __syncthreads();
+      stop = s_next == 0;
+      __syncthreads();
+      ++t;
+    }
+    const Cand b = s_best;
+    if (!b.valid) {
+      if (threadIdx.x == 0) write_leaf(a.res, node);
+    } else {
+      if (threadIdx.x == 0)
+        write_result(a.res, a.res_cnt, a.Cmax, node, b, P.task == 0 ? s_bestL : nullptr, C);
+      cta_partition<BLOCK>(a.rowsA, a.wA, a.rowsB, a.wB, nd.ebeg, m, b.nl_e,
+                           P.X + (long long)b.f * P.N, b.thr, s_scan);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace dml

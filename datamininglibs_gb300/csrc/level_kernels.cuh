@@ -1,0 +1,616 @@
+// Tiny-node warp kernel, root construction, level scans and model emission.
+#pragma once
+#include "fit_kernels.cuh"
+
+namespace dml {
+
+// ============================================================== tiny nodes
+// One warp per node with at most 32 entries: entries live in lanes.  RF sorts
+// the 32 (key, lane) pairs with a register bitonic network; prefix class
+// counts come from warp scans.  Same candidate rules as the CTA kernels.
+template <int CW>
+__global__ void __launch_bounds__(256) k_warp_nodes(LevelArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int wi = gw; wi < a.nwork; wi += nwarps) {
+    const int node = a.work[wi];
+    const LNode nd = a.nodes[node];
+    const ProbDesc& P = a.probs[nd.prob];
+    const int C = P.C;
+    const int m = nd.ecnt;
+    const bool valid = lane < m;
+    const int* rows = a.rowsA + nd.ebeg;
+    const int* ncnt = a.cnt + (long long)node * a.Cmax;
+    const int ml = max(1, P.min_leaf);
+    const int row = valid ? __ldg(rows + lane) : 0;
+    const int w = valid ? (a.wA ? __ldg(a.wA + nd.ebeg + lane) : 1) : 0;
+    const int k = (valid && P.task == 0) ? __ldg(P.lab + row) : -1;
+    const long long qv = (valid && P.task == 1) ? __ldg(P.q + row) : 0;
+    ff prior{0.0f, 0.0f};
+    if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
+    Cand best;
+    best.valid = 0;
+    int bestL = 0;  // lane c holds the best split's left count of class c
+    for (int t = 0;; ++t) {
+      const int f = feature_of_try(P, nd, t);
+      const float* xf = P.X + (long long)f * P.N;
+      const float xv = valid ? __ldg(xf + row) : 0.0f;
+      Cand cd;
+      cd.f = f;
+      int myL = 0;
+      if (P.algo == 1) {  // ERT
+        float sv = 0.0f;
+        if (lane < 10) {
+          U4 r = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)nd.tree,
+                       (uint32_t)nd.idx, (uint32_t)(t * 3 + lane / 4));
+          uint32_t pos = pick(r, lane & 3) % (uint32_t)m;
+          sv = __ldg(xf + __ldg(rows + pos));
+        }
+        float acc = 0.0f;
+        for (int s = 0; s < 10; ++s) acc = __fadd_rn(acc, __shfl_sync(kFull, sv, s));
+        const float thr = __fdiv_rn(acc, 10.0f);
+        const bool left = valid && goes_left(xv, thr);
+        const unsigned lm = __ballot_sync(kFull, left);
+        const long long nl = __popc(lm);
+        const long long nr = (long long)nd.n - nl;
+        cd.thr = thr;
+        cd.nl_e = (int)nl;
+        cd.nl = (int)nl;
+        cd.suml = 0;
+        cd.valid = nl >= ml && nr >= ml;
+        if (P.task == 0) {
+          for (int c = 0; c < C; ++c) {
+            unsigned mc = __ballot_sync(kFull, k == c);
+            if (lane == c) myL = __popc(mc & lm);
+          }
+          cd.gain = cd.valid ? entropy_gain(
+                                   a.H, prior, C, nl, nr,
+                                   [&](int c) { return (long long)__shfl_sync(kFull, myL, c); },
+                                   [&](int c) { return (long long)ncnt[c]; })
+                             : -FLT_MAX;
+        } else {
+          long long sl = warp_sum<long long>(left ? qv : 0);
+          cd.suml = sl;
+          cd.gain = cd.valid ? variance_gain(nl, sl, nr, nd.sum - sl, P.S) : -FLT_MAX;
+        }
+      } else {  // RF: bitonic sort of (key, lane)
+        uint32_t key = valid ? orderable(xv) : 0xFFFFFFFFu;
+        int idx = lane;
+#pragma unroll
+        for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+          for (int j = kk >> 1; j > 0; j >>= 1) {
+            uint32_t pk = __shfl_xor_sync(kFull, key, j);
+            int pi = __shfl_xor_sync(kFull, idx, j);
+            bool up = (lane & kk) == 0;
+            bool lower = (lane & j) == 0;
+            bool mine_smaller = key < pk || (key == pk && idx < pi);
+            bool keep = (lower == up) ? mine_smaller : !mine_smaller;
+            if (!keep) {
+              key = pk;
+              idx = pi;
+            }
+          }
+        }
+        // lane p now holds sorted position p, originally lane idx
+        const int ke = __shfl_sync(kFull, k, idx);
+        const int we = __shfl_sync(kFull, w, idx);
+        const long long qe = __shfl_sync(kFull, qv, idx);
+        const float xe = __shfl_sync(kFull, xv, idx);
+        const uint32_t prevk = __shfl_up_sync(kFull, key, 1);
+        const float prevx = __shfl_up_sync(kFull, xe, 1);
+        const long long nl = warp_excl_scan<long long>(we);
+        const long long nr = (long long)nd.n - nl;
+        bool bnd = lane > 0 && lane < m && prevk < key && nl >= ml && nr >= ml;
+        float g = -FLT_MAX;
+        long long sl = 0;
+        int L[2 * CW];
+        if (P.task == 0) {
+#pragma unroll
+          for (int c = 0; c < 2 * CW; ++c)
+            L[c] = c < C ? warp_excl_scan<int>(ke == c ? we : 0) : 0;
+          if (bnd)
+            g = entropy_gain(
+                a.H, prior, C, nl, nr,
+                [&](int c) {
+                  int x = L[0];
+#pragma unroll
+                  for (int j = 1; j < 2 * CW; ++j)
+                    if (c == j) x = L[j];
+                  return (long long)x;
+                },
+                [&](int c) { return (long long)ncnt[c]; });
+        } else {
+          sl = warp_excl_scan<long long>(qe * (long long)we);
+          if (bnd) g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
+        }
+        // warp argmax: valid, higher gain, lower position
+        int bp = bnd ? lane : -1;
+        float bg = g;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          float g2 = __shfl_xor_sync(kFull, bg, o);
+          int p2 = __shfl_xor_sync(kFull, bp, o);
+          bool take = p2 >= 0 && (bp < 0 || g2 > bg || (g2 == bg && p2 < bp));
+          if (take) {
+            bg = g2;
+            bp = p2;
+          }
+        }
+        if (bp >= 0) {
+          cd.valid = 1;
+          cd.gain = bg;
+          float xa = __shfl_sync(kFull, prevx, bp);
+          float xb = __shfl_sync(kFull, xe, bp);
+          cd.thr = midpoint_threshold(xa, xb);
+          cd.nl_e = bp;
+          cd.nl = (int)__shfl_sync(kFull, nl, bp);
+          cd.suml = __shfl_sync(kFull, sl, bp);
+          if (P.task == 0) {
+            // lane c takes the class-c count of position bp
+            int mine = 0;
+#pragma unroll
+            for (int c = 0; c < 2 * CW; ++c) {
+              int v = __shfl_sync(kFull, L[c], bp);
+              if (lane == c) mine = v;
+            }
+            myL = mine;
+          }
+        } else {
+          cd.valid = 0;
+          cd.gain = -FLT_MAX;
+          cd.thr = 0.0f;
+          cd.nl_e = cd.nl = 0;
+          cd.suml = 0;
+        }
+      }
+      // try-loop decision (uniform across the warp)
+      bool more;
+      if (t < P.n_mand) {
+        if (t == 0 || better(cd, best)) {
+          best = cd;
+          bestL = myL;
+        }
+        more = (t + 1 < P.n_mand) || (P.n_opt > 0 && !(best.valid && best.gain >= kSensible));
+      } else {
+        if (better(cd, best)) {
+          best = cd;
+          bestL = myL;
+        }
+        more = !(cd.valid && cd.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
+      }
+      if (!more) break;
+    }
+    if (!best.valid) {
+      if (lane == 0) write_leaf(a.res, node);
+      continue;
+    }
+    if (lane == 0) write_result(a.res, a.res_cnt, a.Cmax, node, best, nullptr, 0);
+    if (P.task == 0 && lane < C) a.res_cnt[(long long)node * a.Cmax + lane] = bestL;
+    // stable partition with one ballot
+    const float xb = valid ? __ldg(P.X + (long long)best.f * P.N + row) : 0.0f;
+    const bool left = valid && goes_left(xb, best.thr);
+    const unsigned lm = __ballot_sync(kFull, left);
+    if (valid) {
+      int pos = __popc(lm & lt);
+      long long dst = nd.ebeg + (left ? pos : best.nl_e + (lane - pos));
+      a.rowsB[dst] = row;
+      if (a.wB) a.wB[dst] = w;
+    }
+  }
+}
+
+// ============================================================ work queues
+// Node classes: tiny (<= 32 entries, warp), ERT (CTA), RF small (CTA, shared
+// memory sort), RF big (CTA, global sort).  Queue order does not affect
+// results, only scheduling.
+enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kNumQ = 4 };
+
+struct Queues {
+  int* list[kNumQ];
+  int* count;  // [kNumQ]
+  int rf_small_cap;
+};
+
+// Warp-aggregated append of `node` to queue q (all lanes call; `want` selects).
+__device__ __forceinline__ void enqueue(Queues Q, int q, int node, bool want) {
+  for (int qq = 0; qq < kNumQ; ++qq) {
+    bool mine = want && q == qq;
+    unsigned m = __ballot_sync(kFull, mine);
+    if (m == 0) continue;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&Q.count[qq], __popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    if (mine) Q.list[qq][base + __popc(m & ((1u << lane) - 1u))] = node;
+  }
+}
+
+__device__ __forceinline__ int queue_of(const ProbDesc& P, int ecnt, int small_cap) {
+  if (ecnt <= 32) return kQWarp;
+  if (P.algo == 1) return kQErt;
+  return ecnt <= small_cap ? kQRfSmall : kQRfBig;
+}
+
+__device__ __forceinline__ bool preleaf(const ProbDesc& P, int n, int depth) {
+  return n <= P.min_node_size || depth >= P.max_depth;
+}
+
+// ============================================================ roots
+// RF bootstrap multiplicities: row r of tree t is drawn w[r] times among the
+// N draws keyed (seed, tree, i) (gpurf.cu:101-113 with keyed draws).
+__global__ void k_boot_count(const ProbDesc* probs, const int* tree_prob, int* wcnt,
+                             int chunk) {
+  const int gt = blockIdx.y;
+  const ProbDesc& P = probs[tree_prob[gt]];
+  if (P.algo != 0) return;
+  const int t = gt - P.tree0;
+  long long slot0 = P.ent0 + (long long)t * P.N;
+  long long beg = (long long)blockIdx.x * chunk;
+  long long end = min(P.N, beg + chunk);
+  for (long long i = beg + threadIdx.x; i < end; i += blockDim.x) {
+    U4 r = keyed(P.seed, kTagBoot, 0, (uint32_t)t, (uint32_t)(i >> 2), (uint32_t)(i >> 34));
+    uint32_t row = pick(r, (int)(i & 3)) % (uint32_t)P.N;
+    atomicAdd(&wcnt[slot0 + row], 1);
+  }
+}
+
+// One CTA per tree: compact the rows with non-zero weight (ascending) into
+// the entry slots and build the root node.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_roots(const ProbDesc* probs, const int* tree_prob,
+                                                 const int* wcnt, int* rows, int* wts,
+                                                 LNode* nodes, int* cnt, int Cmax, NodeRes* res,
+                                                 Queues Q) {
+  __shared__ int sm[BLOCK / 32];
+  __shared__ int s_cnt[kMaxClasses];
+  __shared__ unsigned long long s_sum;
+  __shared__ unsigned long long s_n;
+  const int gt = blockIdx.x;
+  const int pi = tree_prob[gt];
+  const ProbDesc& P = probs[pi];
+  const int t = gt - P.tree0;
+  const long long slot0 = P.ent0 + (long long)t * P.N;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < kMaxClasses) s_cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) {
+    s_sum = 0;
+    s_n = 0;
+  }
+  __syncthreads();
+  int out = 0;
+  for (long long base = 0; base < P.N; base += BLOCK) {
+    long long r = base + threadIdx.x;
+    int w = 0;
+    if (r < P.N) w = P.algo == 0 ? wcnt[slot0 + r] : 1;
+    int tot;
+    int pos = block_excl_scan<BLOCK, int>(w > 0 ? 1 : 0, &tot, sm);
+    if (w > 0) {
+      rows[slot0 + out + pos] = (int)r;
+      if (wts) wts[slot0 + out + pos] = w;
+    }
+    out += tot;
+    unsigned long long wn = warp_sum<unsigned long long>((unsigned long long)w);
+    if (lane == 0) atomicAdd(&s_n, wn);
+    if (P.task == 0) {
+      int k = (w > 0) ? __ldg(P.lab + r) : -1;
+      for (int c = 0; c < P.C; ++c) {
+        int s = warp_sum<int>(k == c ? w : 0);
+        if (lane == 0 && s) atomicAdd(&s_cnt[c], s);
+      }
+    } else {
+      long long s = warp_sum<long long>(w > 0 ? __ldg(P.q + r) * (long long)w : 0);
+      if (lane == 0 && s) atomicAdd(&s_sum, (unsigned long long)s);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    LNode nd;
+    nd.prob = pi;
+    nd.tree = t;
+    nd.idx = 0;
+    nd.depth = 0;
+    nd.tstart = gt;
+    nd.fstart = P.tree0;
+    nd.fend = P.tree0 + P.n_trees;
+    nd.ecnt = out;
+    nd.ebeg = slot0;
+    nd.n = (int)s_n;
+    nd.pad = 0;
+    nd.sum = (long long)s_sum;
+    nodes[gt] = nd;
+    write_leaf(res, gt);
+  }
+  if (threadIdx.x < Cmax) cnt[(long long)gt * Cmax + threadIdx.x] = threadIdx.x < P.C ? s_cnt[threadIdx.x] : 0;
+  if (threadIdx.x < 32) {
+    bool want = threadIdx.x == 0 && !preleaf(P, (int)s_n, 0);
+    enqueue(Q, queue_of(P, out, Q.rf_small_cap), gt, want);
+  }
+}
+
+// ============================================================ level scans
+// Exclusive scans over the level of (2 if split) and (1 if leaf): child and
+// leaf positions.  pos arrays have n+1 entries (the last holds the totals).
+constexpr int kScanBlock = 1024;
+constexpr int kScanItems = 4;
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_part(const NodeRes* res, int n, int2* part) {
+  __shared__ int sm[kScanBlock / 32];
+  long long base = (long long)blockIdx.x * kScanBlock * kScanItems;
+  int c = 0, l = 0;
+  for (int it = 0; it < kScanItems; ++it) {
+    long long j = base + (long long)it * kScanBlock + threadIdx.x;
+    if (j < n) {
+      int s = res[j].split;
+      c += 2 * s;
+      l += 1 - s;
+    }
+  }
+  int tc, tl;
+  block_excl_scan<kScanBlock, int>(c, &tc, sm);
+  block_excl_scan<kScanBlock, int>(l, &tl, sm);
+  if (threadIdx.x == 0) part[blockIdx.x] = make_int2(tc, tl);
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_top(int2* part, int nparts, int* childpos,
+                                                         int* leafpos, int n, int* summary) {
+  __shared__ int sm[kScanBlock / 32];
+  int carry_c = 0, carry_l = 0;
+  for (int base = 0; base < nparts; base += kScanBlock) {
+    int i = base + threadIdx.x;
+    int2 v = i < nparts ? part[i] : make_int2(0, 0);
+    int tc, tl;
+    int ec = block_excl_scan<kScanBlock, int>(v.x, &tc, sm);
+    int el = block_excl_scan<kScanBlock, int>(v.y, &tl, sm);
+    if (i < nparts) part[i] = make_int2(carry_c + ec, carry_l + el);
+    carry_c += tc;
+    carry_l += tl;
+  }
+  if (threadIdx.x == 0) {
+    childpos[n] = carry_c;
+    leafpos[n] = carry_l;
+    summary[0] = carry_c;
+    summary[1] = carry_l;
+  }
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_apply(const NodeRes* res, int n,
+                                                           const int2* part, int* childpos,
+                                                           int* leafpos) {
+  __shared__ int sm[kScanBlock / 32];
+  const long long base = (long long)blockIdx.x * kScanBlock * kScanItems;
+  int2 off = part[blockIdx.x];
+  for (int it = 0; it < kScanItems; ++it) {
+    long long j = base + (long long)it * kScanBlock + threadIdx.x;
+    int s = j < n ? res[j].split : 0;
+    int c = j < n ? 2 * s : 0, l = j < n ? 1 - s : 0;
+    int tc, tl;
+    int ec = block_excl_scan<kScanBlock, int>(c, &tc, sm);
+    int el = block_excl_scan<kScanBlock, int>(l, &tl, sm);
+    if (j < n) {
+      childpos[j] = off.x + ec;
+      leafpos[j] = off.y + el;
+    }
+    off.x += tc;
+    off.y += tl;
+  }
+}
+
+// ============================================================ emission
+struct EmitArgs {
+  const ProbDesc* probs;
+  const LNode* cur;
+  const int* cnt;
+  const NodeRes* res;
+  const int* res_cnt;
+  const int* childpos;
+  const int* leafpos;
+  int n;
+  int Cmax;
+  long long log_base;    // node log position of this level's first node
+  long long plog_base;   // first leaf rank of this level in the probability log
+  ClassifyNode* node_log;
+  float* prob_log;       // Cmax floats per leaf rank
+  const long long* fbase_cur;
+  const long long* lbase_cur;
+  long long* fbase_next;
+  long long* lbase_next;
+  Seg* seg;              // [n_forests] for this level
+  LNode* next;
+  int* next_cnt;
+  NodeRes* next_res;
+  Queues Q;
+  long long* stats;      // [0] entries of open nodes, [1] weighted rows
+};
+
+__global__ void __launch_bounds__(256) k_emit(EmitArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = j < a.n;
+  int qL = 0, qR = 0, cpL = 0, cpR = 0;
+  bool wantL = false, wantR = false;
+  unsigned long long my_e = 0, my_w = 0;
+  if (act) {
+    const LNode nd = a.cur[j];
+    const NodeRes r = a.res[j];
+    const ProbDesc& P = a.probs[nd.prob];
+    const int f = nd.prob;
+    const int fs = nd.fstart, fe = nd.fend;
+    const long long fb = a.fbase_cur[f], lb = a.lbase_cur[f];
+    ClassifyNode cn;
+    if (r.split) {
+      const int cp = a.childpos[j];
+      const int cfs = a.childpos[fs];
+      cn.child_start = (int)(fb + (fe - fs) + (cp - cfs));
+      cn.child_count = 2;
+      cn.probability_start = -1;
+      cn.attribute = r.f;
+      cn.split_point = r.thr;
+      LNode L, R;
+      L.prob = R.prob = nd.prob;
+      L.tree = R.tree = nd.tree;
+      L.idx = cp - a.childpos[nd.tstart];
+      R.idx = L.idx + 1;
+      L.depth = R.depth = nd.depth + 1;
+      L.tstart = R.tstart = a.childpos[nd.tstart];
+      L.fstart = R.fstart = cfs;
+      L.fend = R.fend = a.childpos[fe];
+      L.ebeg = nd.ebeg;
+      L.ecnt = r.nl_e;
+      R.ebeg = nd.ebeg + r.nl_e;
+      R.ecnt = nd.ecnt - r.nl_e;
+      L.n = r.nl;
+      R.n = nd.n - r.nl;
+      L.pad = R.pad = 0;
+      L.sum = r.suml;
+      R.sum = nd.sum - r.suml;
+      a.next[cp] = L;
+      a.next[cp + 1] = R;
+      for (int c = 0; c < a.Cmax; ++c) {
+        int lc = (P.task == 0 && c < P.C) ? a.res_cnt[(long long)j * a.Cmax + c] : 0;
+        int tc = (P.task == 0 && c < P.C) ? a.cnt[(long long)j * a.Cmax + c] : 0;
+        a.next_cnt[(long long)cp * a.Cmax + c] = lc;
+        a.next_cnt[(long long)(cp + 1) * a.Cmax + c] = tc - lc;
+      }
+      write_leaf(a.next_res, cp);
+      write_leaf(a.next_res, cp + 1);
+      cpL = cp;
+      cpR = cp + 1;
+      wantL = !preleaf(P, L.n, L.depth);
+      wantR = !preleaf(P, R.n, R.depth);
+      qL = queue_of(P, L.ecnt, a.Q.rf_small_cap);
+      qR = queue_of(P, R.ecnt, a.Q.rf_small_cap);
+    } else {
+      const long long lr = lb + (a.leafpos[j] - a.leafpos[fs]);
+      cn.child_start = -1;
+      cn.child_count = 0;
+      cn.probability_start = (int)(lr * (long long)P.C);
+      cn.attribute = -1;
+      cn.split_point = -1.0f;
+      float* dst = a.prob_log + (a.plog_base + a.leafpos[j]) * (long long)a.Cmax;
+      if (P.task == 0) {
+        for (int c = 0; c < P.C; ++c) dst[c] = (float)a.cnt[(long long)j * a.Cmax + c];
+      } else {
+        double v = ((double)nd.sum * pow2d(-P.S)) / (double)nd.n;
+        dst[0] = __double2float_rn(v);
+      }
+    }
+    a.node_log[a.log_base + j] = cn;
+    if (j == fs) {
+      a.fbase_next[f] = fb + (fe - fs);
+      a.lbase_next[f] = lb + (a.leafpos[fe] - a.leafpos[fs]);
+      Seg s;
+      s.node_pos = a.log_base + fs;
+      s.node_cnt = fe - fs;
+      s.pad = 0;
+      s.leaf_rank = a.plog_base + a.leafpos[fs];
+      s.leaf_cnt = a.leafpos[fe] - a.leafpos[fs];
+      a.seg[f] = s;
+    }
+    my_e = (unsigned long long)nd.ecnt;
+    my_w = (unsigned long long)nd.n;
+  }
+  my_e = warp_sum<unsigned long long>(my_e);
+  my_w = warp_sum<unsigned long long>(my_w);
+  if ((threadIdx.x & 31) == 0 && my_e) {
+    atomicAdd((unsigned long long*)&a.stats[0], my_e);
+    atomicAdd((unsigned long long*)&a.stats[1], my_w);
+  }
+  enqueue(a.Q, qL, cpL, wantL);
+  enqueue(a.Q, qR, cpR, wantR);
+}
+
+// ============================================================ data prep
+// Checks the frame (finite features, integral labels in [0, C)) and gathers
+// max |y| for the regression fixed-point scale.  err bits: 1 = non-finite
+// feature, 2 = bad label, 4 = non-finite target.
+__global__ void k_validate(const float* X, long long nX, const float* y, long long N, int task,
+                           int C, int* err, unsigned* maxabs) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  int e = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nX; i += stride) {
+    float x = X[i];
+    if (!isfinite(x)) e |= 1;
+  }
+  unsigned mx = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    float v = y[i];
+    if (task == 0) {
+      if (!(v >= 0.0f && v < (float)C && v == truncf(v))) e |= 2;
+    } else {
+      if (!isfinite(v)) e |= 4;
+      mx = max(mx, __float_as_uint(fabsf(v)));
+    }
+  }
+  if (e) atomicOr(err, e);
+  if (task == 1) atomicMax(maxabs, mx);
+}
+
+__global__ void k_prep_targets(const float* y, long long N, int task, int S, int* lab,
+                               long long* q) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  const double sc = pow2d(S);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    if (task == 0)
+      lab[i] = (int)y[i];
+    else
+      q[i] = __double2ll_rn((double)y[i] * sc);
+  }
+}
+
+// Probabilities from the strided log into a forest's packed array, and the
+// nodes of each (level, forest) segment into the forest's node array.
+__global__ void k_gather_nodes(const ClassifyNode* log, long long pos, int cnt, ClassifyNode* dst) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    dst[i] = log[pos + i];
+}
+__global__ void k_gather_probs(const float* plog, long long rank0, long long cnt, int Cmax, int C,
+                               float* dst) {
+  long long total = cnt * C;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long l = i / C;
+    int c = (int)(i % C);
+    dst[i] = plog[(rank0 + l) * Cmax + c];
+  }
+}
+
+// Predict layout from the Classify layout: the voted class of each leaf
+// (first class with the strictly largest count, gpudte.cu:340-352) is
+// precomputed; regression leaves carry their value.
+__global__ void k_to_pnodes(const ClassifyNode* nodes, long long n, const float* probs, int C,
+                            int task, PNode* out) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    ClassifyNode cn = nodes[i];
+    PNode p;
+    p.pad = 0;
+    if (cn.child_count > 0) {
+      p.a = cn.child_start;
+      p.b = cn.attribute;
+      p.t = cn.split_point;
+    } else {
+      const float* pr = probs + cn.probability_start;
+      p.a = -1;
+      if (task == 0) {
+        int sel = 0;
+        float mx = 0.0f;
+        for (int c = 0; c < C; ++c)
+          if (pr[c] > mx) {
+            mx = pr[c];
+            sel = c;
+          }
+        p.b = sel;
+        p.t = 0.0f;
+      } else {
+        p.b = 0;
+        p.t = pr[0];
+      }
+    }
+    out[i] = p;
+  }
+}
+
+}  // namespace dml

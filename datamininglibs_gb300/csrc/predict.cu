@@ -1,0 +1,228 @@
+// Forest prediction and the forest handle entry points.
+//
+// Replaces GpuDteAlgorithm<T>::Predict (lib_ensembles/source/gpudte_algorithm.cc:
+// 270-331) and gpudte_predict (lib_ensembles/source/gpudte.cu:311-359): the
+// reference launches one thread per (tree, row), in chunks of 65,536 with a
+// device sync each, and adds every vote to global memory with an atomic.  Here
+// a thread owns a row for all trees: it walks each tree over the 16-byte
+// predict layout (leaf votes precomputed), counts votes in shared memory and
+// writes its row once.  Tree order is fixed, so regression sums are
+// deterministic.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "dml_device.cuh"
+#include "engine.h"
+
+namespace dml {
+
+const char* last_error_str();
+void clear_error();
+void init_pool_once();
+
+constexpr int kPredBlock = 128;
+
+// Rows are walked through all trees; a tile of the row's features is not
+// staged because each row reads only the features on its paths.
+template <int TASK>
+__global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict__ nodes,
+                                                        int n_trees, int C,
+                                                        const float* __restrict__ X, long long N,
+                                                        float* __restrict__ out) {
+  extern __shared__ int votes[];  // [kPredBlock][C]
+  const long long row = (long long)blockIdx.x * kPredBlock + threadIdx.x;
+  const bool act = row < N;
+  int* my = votes + threadIdx.x * C;
+  if (TASK == 0)
+    for (int c = 0; c < C; ++c) my[c] = 0;
+  float acc = 0.0f;
+  if (act) {
+    for (int t = 0; t < n_trees; ++t) {
+      int4 p = __ldg(reinterpret_cast<const int4*>(nodes) + t);
+      while (p.x >= 0) {
+        float x = __ldg(X + (long long)p.y * N + row);
+        int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
+        p = __ldg(reinterpret_cast<const int4*>(nodes) + nx);
+      }
+      if (TASK == 0)
+        my[p.y] += 1;
+      else
+        acc = __fadd_rn(acc, __int_as_float(p.z));
+    }
+    if (TASK == 0) {
+      for (int c = 0; c < C; ++c) out[row * C + c] = (float)my[c];
+    } else {
+      out[row] = acc;
+    }
+  }
+}
+
+dml_status predict_device(const dml_forest* f, const float* dX, long long n_rows, float* dout,
+                          cudaStream_t s) {
+  if (n_rows <= 0) return DML_OK;
+  const long long blocks = (n_rows + kPredBlock - 1) / kPredBlock;
+  if (f->task == DML_CLASSIFICATION) {
+    size_t sm = sizeof(int) * kPredBlock * f->n_classes;
+    k_predict<0><<<(unsigned)blocks, kPredBlock, sm, s>>>(f->pnodes, f->n_trees, f->n_classes, dX,
+                                                          n_rows, dout);
+  } else {
+    k_predict<1><<<(unsigned)blocks, kPredBlock, 0, s>>>(f->pnodes, f->n_trees, 1, dX, n_rows,
+                                                         dout);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("predict launch failed: %s", cudaGetErrorString(e));
+    return DML_ERR_CUDA;
+  }
+  return DML_OK;
+}
+
+}  // namespace dml
+
+using namespace dml;
+
+extern "C" {
+
+dml_status dml_predict(const dml_forest* f, const float* samples, int64_t n_rows, float* out,
+                       int32_t memory, void* stream) {
+  clear_error();
+  if (!f || (!samples && n_rows > 0) || (!out && n_rows > 0) || n_rows < 0 ||
+      (memory != DML_HOST && memory != DML_DEVICE)) {
+    set_error("invalid predict arguments");
+    return DML_ERR_INVALID_ARG;
+  }
+  if (n_rows == 0) return DML_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long width = f->task == DML_CLASSIFICATION ? f->n_classes : 1;
+  if (memory == DML_DEVICE) {
+    dml_status st = predict_device(f, samples, n_rows, out, s);
+    return st;
+  }
+  init_pool_once();
+  float* dX = nullptr;
+  float* dout = nullptr;
+  size_t xb = sizeof(float) * (size_t)n_rows * f->n_features;
+  size_t ob = sizeof(float) * (size_t)n_rows * width;
+  if (cudaMallocAsync(&dX, xb, s) != cudaSuccess || cudaMallocAsync(&dout, ob, s) != cudaSuccess) {
+    cudaGetLastError();
+    if (dX) cudaFreeAsync(dX, s);
+    set_error("device allocation failed for a predict of %lld rows", (long long)n_rows);
+    return DML_ERR_OOM;
+  }
+  dml_status st = DML_OK;
+  if (cudaMemcpyAsync(dX, samples, xb, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("host to device copy failed");
+    st = DML_ERR_CUDA;
+  }
+  if (st == DML_OK) st = predict_device(f, dX, n_rows, dout, s);
+  if (st == DML_OK && cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+    set_error("device to host copy failed");
+    st = DML_ERR_CUDA;
+  }
+  cudaFreeAsync(dX, s);
+  cudaFreeAsync(dout, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (st == DML_OK && e != cudaSuccess) {
+    set_error("predict failed: %s", cudaGetErrorString(e));
+    st = DML_ERR_CUDA;
+  }
+  return st;
+}
+
+dml_status dml_forest_info_get(const dml_forest* f, dml_forest_info* info) {
+  if (!f || !info) {
+    set_error("null argument");
+    return DML_ERR_INVALID_ARG;
+  }
+  std::memset(info, 0, sizeof(*info));
+  info->task = f->task;
+  info->n_trees = f->n_trees;
+  info->n_classes = f->n_classes;
+  info->n_features = f->n_features;
+  info->n_nodes = f->n_nodes;
+  info->n_probs = f->n_probs;
+  info->max_depth = f->max_depth;
+  info->fit_ms = f->fit_ms;
+  return DML_OK;
+}
+
+dml_status dml_forest_export(const dml_forest* f, void* node_array, float* probs) {
+  clear_error();
+  if (!f || (!node_array && f->n_nodes) || (!probs && f->n_probs)) {
+    set_error("null argument");
+    return DML_ERR_INVALID_ARG;
+  }
+  if (cudaMemcpy(node_array, f->nodes, sizeof(ClassifyNode) * f->n_nodes, cudaMemcpyDeviceToHost) !=
+          cudaSuccess ||
+      cudaMemcpy(probs, f->probs, sizeof(float) * f->n_probs, cudaMemcpyDeviceToHost) !=
+          cudaSuccess) {
+    set_error("device to host copy failed");
+    return DML_ERR_CUDA;
+  }
+  return DML_OK;
+}
+
+dml_status dml_forest_import(int32_t task, int32_t n_trees, int32_t n_classes, int32_t n_features,
+                             const void* node_array, int64_t n_nodes, const float* probs,
+                             int64_t n_probs, dml_forest** out) {
+  clear_error();
+  if (!out || !node_array || !probs || n_trees <= 0 || n_nodes < n_trees || n_features <= 0 ||
+      (task != DML_CLASSIFICATION && task != DML_REGRESSION) ||
+      (task == DML_CLASSIFICATION && (n_classes < 1 || n_classes > kMaxClasses))) {
+    set_error("invalid forest import arguments");
+    return DML_ERR_INVALID_ARG;
+  }
+  const int C = task == DML_CLASSIFICATION ? n_classes : 1;
+  // structural checks (the reference's "Faulty gpu node" check, gpudte_algorithm.cc:60-63)
+  const ClassifyNode* nodes = (const ClassifyNode*)node_array;
+  for (long long i = 0; i < n_nodes; ++i) {
+    const ClassifyNode& n = nodes[i];
+    if (n.child_count > 0) {
+      if (n.child_count != 2 || n.child_start <= i || n.child_start + 1 >= n_nodes ||
+          n.attribute < 0 || n.attribute >= n_features) {
+        set_error("node %lld is malformed", i);
+        return DML_ERR_INVALID_ARG;
+      }
+    } else if (n.probability_start < 0 || n.probability_start + C > n_probs) {
+      set_error("leaf %lld points outside the probability array", i);
+      return DML_ERR_INVALID_ARG;
+    }
+  }
+  dml_forest* f = new dml_forest();
+  f->task = task;
+  f->n_trees = n_trees;
+  f->n_classes = C;
+  f->n_features = n_features;
+  f->n_nodes = n_nodes;
+  f->n_probs = n_probs;
+  cudaGetDevice(&f->device);
+  if (cudaMalloc(&f->nodes, sizeof(ClassifyNode) * n_nodes) != cudaSuccess ||
+      cudaMalloc(&f->probs, sizeof(float) * std::max<int64_t>(1, n_probs)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(f->nodes);
+    delete f;
+    set_error("device allocation failed");
+    return DML_ERR_OOM;
+  }
+  cudaMemcpy(f->nodes, node_array, sizeof(ClassifyNode) * n_nodes, cudaMemcpyHostToDevice);
+  cudaMemcpy(f->probs, probs, sizeof(float) * n_probs, cudaMemcpyHostToDevice);
+  dml_status st = forest_build_pnodes(f, 0);
+  if (st == DML_OK && cudaDeviceSynchronize() != cudaSuccess) st = DML_ERR_CUDA;
+  if (st != DML_OK) {
+    dml_forest_free(f);
+    return st;
+  }
+  *out = f;
+  return DML_OK;
+}
+
+void dml_forest_free(dml_forest* f) {
+  if (!f) return;
+  cudaFree(f->nodes);
+  cudaFree(f->probs);
+  cudaFree(f->pnodes);
+  delete f;
+}
+
+}  // extern "C"

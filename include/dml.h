@@ -1,0 +1,189 @@
+/* dml.h — C ABI of the GB300 random-forest / extremely-randomized-trees engine.
+ *
+ * Drop-in boundary for the fit/predict path of novelari/DataminingLibs
+ * (lib_ensembles).  Plain C types only: pointers, sizes, status codes; CUDA
+ * streams are passed as `void*` (a cudaStream_t, or NULL for the default
+ * stream).  No entry point throws; every one returns a dml_status and leaves a
+ * message for dml_last_error() (per calling thread).
+ *
+ * Data layout (lib_data): samples are feature-major, samples[f * n_rows + i]
+ * (lib_parsing/source/csv_parser.cc:92-96, lib_ensembles/source/gpudte.cu:65-68);
+ * targets hold one float per row: the class index as a float for
+ * classification (MlDataFrame<float>::GetTargets), the value for regression.
+ *
+ * Model layout (lib_models): dml_forest_export writes the reference's
+ * kNodeArray of gpuDTE_NodeHeader_Classify<float> = {int child_start,
+ * child_count, probability_start, attribute; float split_point}
+ * (lib_ensembles/source/gpudte_algorithm_shared.h:82-90) with the roots of the
+ * trees at 0..n_trees-1, and kProbArray with n_classes floats per leaf (class
+ * counts) or one float per leaf (regression mean).
+ */
+#ifndef DML_H_
+#define DML_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define DML_API __attribute__((visibility("default")))
+#else
+#define DML_API
+#endif
+
+typedef enum {
+  DML_OK = 0,
+  DML_ERR_INVALID_ARG = 1,
+  DML_ERR_OOM = 2,
+  DML_ERR_CUDA = 3,
+  DML_ERR_TIMEOUT = 4,
+  DML_ERR_BUDGET = 5,
+  DML_ERR_NOT_READY = 6,
+  DML_ERR_INTERNAL = 7
+} dml_status;
+
+/* EnsemblesInterface::CreateGpuRfAlgorithm / CreateGpuErtAlgorithm
+ * (lib_ensembles/source/ensembles_interface.cc:14-26). */
+typedef enum { DML_ALGO_RF = 0, DML_ALGO_ERT = 1 } dml_algo;
+/* AlgorithmsInterface::AlgorithmType (lib_algorithms/include/algorithms_interface.h:9). */
+typedef enum { DML_CLASSIFICATION = 0, DML_REGRESSION = 1 } dml_task;
+/* Where the pointers of a call live. */
+typedef enum { DML_HOST = 0, DML_DEVICE = 1 } dml_memory;
+
+/* Fit parameters and data: the EnsemblesLib DteParams (ensembles_interface.h:28-38)
+ * plus the data frame.  n_features_try = kNrFeatures (0 -> round(ln F) + 1),
+ * max_depth = kMaxDepth, min_node_size = kMinNodeSize, n_trees = kNrTrees,
+ * task = kAlgoType.  min_leaf (>= 1) and seed are additions. */
+typedef struct {
+  int32_t algo;
+  int32_t task;
+  int32_t n_trees;
+  int32_t n_features_try;
+  int32_t max_depth;
+  int32_t min_node_size;
+  int32_t min_leaf;
+  int32_t n_classes; /* classification: labels are 0..n_classes-1; <= 32 */
+  uint64_t seed;
+  int64_t n_rows;
+  int32_t n_features;
+  int32_t memory; /* dml_memory of samples/targets */
+  const float* samples;
+  const float* targets;
+} dml_fit_desc;
+
+typedef struct dml_forest dml_forest;
+
+typedef struct {
+  int32_t task;
+  int32_t n_trees;
+  int32_t n_classes; /* 1 for regression */
+  int32_t n_features;
+  int64_t n_nodes;
+  int64_t n_probs;
+  int32_t max_depth; /* deepest level reached */
+  int32_t reserved;
+  double fit_ms;     /* device time of the level loop of the fit that built it */
+} dml_forest_info;
+
+/* Fit statistics of the last dml_fit/dml_fit_batched on this thread. */
+typedef struct {
+  int64_t nodes;       /* internal + leaf nodes created, all forests */
+  int64_t entries;     /* sum over levels of the open nodes' row entries */
+  int64_t weighted_rows; /* sum over levels of the open nodes' weighted rows */
+  int32_t levels;
+  int32_t launches;    /* kernel launches of the fit */
+  double level_loop_ms; /* device time of the level loop (CUDA events) */
+  double search_ms;     /* device time in the split-search kernels */
+} dml_fit_stats;
+
+/* GpuDteAlgorithm<T>::Fit (lib_ensembles/source/gpudte_algorithm.cc:15-267),
+ * reached through MlAlgorithm<T>::Fit (lib_algorithms/include/ml_algorithm.h:29-30).
+ * Builds the forest on the current device; *out is a device-resident handle. */
+DML_API dml_status dml_fit(const dml_fit_desc* desc, dml_forest** out, void* stream);
+
+/* No reference counterpart as one call: n independent forests (uneven row,
+ * feature and class counts) built together, one launch set per tree level for
+ * all of them.  out[i] receives forest i. */
+DML_API dml_status dml_fit_batched(int32_t n, const dml_fit_desc* descs, dml_forest** out,
+                                   void* stream);
+
+/* The per-level chunked launch structure of the reference
+ * (gpudte_algorithm.cc:145-253: <= 512 nodes per launch, host syncs per chunk),
+ * on this engine's kernels: same results as dml_fit.  The baseline that the
+ * batched level path is measured against. */
+DML_API dml_status dml_fit_plain(const dml_fit_desc* desc, dml_forest** out, void* stream);
+
+DML_API dml_status dml_last_fit_stats(dml_fit_stats* stats);
+
+/* GpuDteAlgorithm<T>::Predict (gpudte_algorithm.cc:270-331).  samples is
+ * feature-major [n_features * n_rows]; out receives n_rows * n_classes vote
+ * counts (classification) or n_rows sums of tree outputs (regression), as
+ * MlResultData::AddPredictions holds them (ml_resultdata_impl.cc:17-21). */
+DML_API dml_status dml_predict(const dml_forest* forest, const float* samples, int64_t n_rows,
+                               float* out, int32_t memory, void* stream);
+
+DML_API dml_status dml_forest_info_get(const dml_forest* forest, dml_forest_info* info);
+
+/* The model slots kNodeArray / kProbArray (lib_models/include/models_interface.h:9-19,
+ * filled at gpudte_algorithm.cc:257-258).  node_array receives n_nodes * 20
+ * bytes, probs n_probs floats (host memory). */
+DML_API dml_status dml_forest_export(const dml_forest* forest, void* node_array, float* probs);
+
+/* A device-resident forest from kNodeArray / kProbArray in the layout above
+ * (host memory), e.g. a model built by the reference or merged on the host. */
+DML_API dml_status dml_forest_import(int32_t task, int32_t n_trees, int32_t n_classes,
+                                     int32_t n_features, const void* node_array, int64_t n_nodes,
+                                     const float* probs, int64_t n_probs, dml_forest** out);
+
+DML_API void dml_forest_free(dml_forest* forest);
+
+DML_API const char* dml_last_error(void);
+
+/* ------------------------------------------------------------------ serving
+ * No reference counterpart (the reference has no serving path): a resident-
+ * forest prediction server with continuous batching.  Requests of 1..65536 rows
+ * are admitted while earlier ones run, as HBM budget and batch slots free up;
+ * their work shares kernel launches across streams. */
+typedef struct dml_server dml_server;
+
+typedef struct {
+  int64_t hbm_budget_bytes;   /* device bytes for request inputs/outputs */
+  int32_t max_batch_rows;     /* rows packed into one launch */
+  int32_t n_streams;          /* launches in flight */
+  int32_t max_wait_us;        /* how long a batch waits to fill */
+  int32_t reserved;
+} dml_server_config;
+
+typedef struct {
+  int64_t completed;
+  int64_t rows;
+  double p50_ms;
+  double p99_ms;
+  double mean_ms;
+  double rows_per_s;
+  int64_t launches;
+  int64_t rejected;
+} dml_server_stats;
+
+DML_API dml_status dml_server_create(const dml_server_config* cfg, dml_server** out);
+/* The forest stays owned by the caller and must outlive the server. */
+DML_API dml_status dml_server_add_forest(dml_server* s, const dml_forest* forest, int32_t* forest_id);
+/* samples: host feature-major [n_features * n_rows]; out: host buffer of
+ * n_rows * width floats, written when the request completes.  Both must stay
+ * valid until dml_server_poll reports the request done. */
+DML_API dml_status dml_server_submit(dml_server* s, int32_t forest_id, const float* samples,
+                                     int64_t n_rows, float* out, int64_t* request_id);
+/* DML_OK when done, DML_ERR_NOT_READY while pending; latency_ms is the time
+ * from submit to completion. */
+DML_API dml_status dml_server_poll(dml_server* s, int64_t request_id, double* latency_ms);
+DML_API dml_status dml_server_wait(dml_server* s, int64_t request_id, double* latency_ms);
+DML_API dml_status dml_server_stats_get(dml_server* s, dml_server_stats* stats);
+DML_API void dml_server_destroy(dml_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DML_H_ */

@@ -1,0 +1,220 @@
+"""CUDA engine vs the oracle through the C ABI: trees, leaf payloads and votes
+bit-exact, regression sums bit-exact (same tree order), on seeded inputs of the
+benchmark distributions at sizes the oracle finishes in seconds, plus the edge
+cases of the reference's path."""
+import numpy as np
+import pytest
+
+import oracle
+from datamininglibs_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+FLT_MAX = np.finfo(np.float32).max
+
+
+@pytest.fixture(scope="module")
+def dml():
+    import datamininglibs_gb300 as d
+    d.lib()
+    return d
+
+
+def _fit_both(dml, X, y, **kw):
+    m = oracle.fit(X, y, **kw)
+    f = dml.fit(X, y, **kw)
+    nodes, probs = f.export()
+    return m, f, nodes, probs
+
+
+def _assert_same_model(m, nodes, probs, tag=""):
+    assert nodes.shape == m.nodes.shape, (tag, nodes.shape, m.nodes.shape)
+    bad = np.nonzero(np.any(nodes != m.nodes, axis=1))[0]
+    assert bad.size == 0, (tag, "first differing node", bad[:5], nodes[bad[:3]], m.nodes[bad[:3]])
+    assert np.array_equal(probs, m.probs), tag
+
+
+CASES = {
+    "ert_cls": (lambda: synth.ert_binary(1500, 21, seed=1),
+                dict(algo=1, n_trees=16, K=7, max_depth=12, min_node_size=10, n_classes=2, seed=0)),
+    "rf_cls": (lambda: synth.rf_multiclass(3000, 24, n_classes=10, n_int=4, seed=2),
+               dict(algo=0, n_trees=12, K=5, max_depth=20, min_node_size=5, min_leaf=2,
+                    n_classes=10, seed=3)),
+    "rf_reg": (lambda: synth.rf_regression(3000, 16, seed=4),
+               dict(algo=0, task=1, n_trees=8, K=6, max_depth=24, min_node_size=5, min_leaf=5,
+                    seed=5)),
+    "ert_reg": (lambda: synth.rf_regression(2000, 12, seed=6),
+                dict(algo=1, task=1, n_trees=8, K=4, max_depth=14, min_node_size=5, seed=7)),
+    "rf_cls_big_nodes": (lambda: synth.rf_multiclass(20000, 12, n_classes=3, n_int=3, seed=8),
+                         dict(algo=0, n_trees=3, K=4, max_depth=8, min_node_size=5,
+                              n_classes=3, seed=9)),
+    "rf_reg_big_nodes": (lambda: synth.rf_regression(12000, 10, seed=10),
+                         dict(algo=0, task=1, n_trees=3, K=4, max_depth=6, min_node_size=5,
+                              seed=11)),
+    "ert_cls_multiclass": (lambda: synth.rf_multiclass(4000, 30, n_classes=7, n_int=5, seed=12),
+                           dict(algo=1, n_trees=10, K=6, max_depth=16, min_node_size=5,
+                                n_classes=7, seed=13)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fit_and_predict_bit_exact(dml, name):
+    gen, kw = CASES[name]
+    X, y = gen()
+    m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+    _assert_same_model(m, nodes, probs, name)
+    pg = f.predict(X)
+    po = oracle.predict(m, X)
+    assert np.array_equal(pg, po), name
+
+
+def test_gains_within_tolerance_of_fp64(dml):
+    """FP32 gains of the chosen splits: the engine's equal the oracle's FP32
+    gains bit for bit (same trees), and those are within 1e-6 relative (plus
+    1e-7 absolute) of the FP64 gains."""
+    X, y = synth.rf_multiclass(3000, 16, n_classes=5, n_int=3, seed=21)
+    kw = dict(algo=0, n_trees=6, K=4, max_depth=14, min_node_size=5, n_classes=5, seed=2)
+    m = oracle.fit(X, y, **kw)
+    ok = ~np.isnan(m.gains32)
+    err = np.abs(m.gains32[ok].astype(np.float64) - m.gains64[ok])
+    assert np.all(err <= 1e-6 * np.abs(m.gains64[ok]) + 1e-7)
+
+
+def test_plain_path_matches_level_path(dml):
+    X, y = synth.rf_multiclass(4000, 20, n_classes=4, n_int=2, seed=31)
+    kw = dict(algo=0, n_trees=6, K=5, max_depth=15, min_node_size=5, n_classes=4, seed=1)
+    a = dml.fit(X, y, **kw).export()
+    b = dml.fit_plain(X, y, **kw).export()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_batched_uneven_forests_match_single_fits(dml):
+    probs = synth.uneven_problems(6, seed=5, n_range=(200, 3000), f_range=(8, 40))
+    specs = []
+    for i, (X, y, c) in enumerate(probs):
+        specs.append(dict(X=X, y=y, algo=1 if i % 3 else 0, n_trees=4, K=0, max_depth=10,
+                          min_node_size=5, n_classes=c, seed=100 + i))
+    specs.append(dict(X=probs[0][0], y=synth.rf_regression(probs[0][0].shape[1], 3, seed=1)[1],
+                      algo=0, task=1, n_trees=3, K=3, max_depth=9, min_node_size=5, seed=7))
+    batch = dml.fit_batched(specs)
+    for sp, fb in zip(specs, batch):
+        sp = dict(sp)
+        X, y = sp.pop("X"), sp.pop("y")
+        m = oracle.fit(X, y, **sp)
+        nodes, pr = fb.export()
+        _assert_same_model(m, nodes, pr)
+
+
+def test_repeated_fits_bitwise_identical(dml):
+    X, y = synth.ert_binary(2500, 20, seed=41)
+    kw = dict(algo=0, n_trees=8, K=5, max_depth=12, min_node_size=5, n_classes=2, seed=4)
+    ref = dml.fit(X, y, **kw).export()
+    for _ in range(2):
+        again = dml.fit(X, y, **kw).export()
+        assert np.array_equal(ref[0], again[0]) and np.array_equal(ref[1], again[1])
+
+
+EDGE = {
+    "root_leaf_depth0": dict(max_depth=0),
+    "min_node_size_huge": dict(min_node_size=10 ** 6),
+    "k_greater_than_f": dict(K=50),
+    "k_equals_f": dict(K=6),
+    "min_leaf_large": dict(min_leaf=40),
+    "single_class": dict(n_classes=1),
+}
+
+
+@pytest.mark.parametrize("name", sorted(EDGE))
+@pytest.mark.parametrize("algo", [0, 1])
+def test_edge_parameters(dml, name, algo):
+    X, y = synth.rf_multiclass(700, 6, n_classes=3, n_int=2, seed=51)
+    kw = dict(algo=algo, n_trees=5, K=3, max_depth=9, min_node_size=4, n_classes=3, seed=8)
+    kw.update(EDGE[name])
+    if kw["n_classes"] == 1:
+        y = np.zeros_like(y)
+    m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+    _assert_same_model(m, nodes, probs, name)
+    assert np.array_equal(f.predict(X), oracle.predict(m, X))
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+def test_missing_values_and_constant_features(dml, algo):
+    X, y = synth.rf_multiclass(1200, 8, n_classes=3, n_int=2, seed=61)
+    X[2] = 1.5                     # constant feature: never splits
+    X[:, ::5] = -FLT_MAX           # missing-value marker goes left
+    X[4, ::3] = 0.0
+    X[4, 1::3] = -0.0              # -0 and +0 are one value
+    kw = dict(algo=algo, n_trees=6, K=4, max_depth=10, min_node_size=4, n_classes=3, seed=3)
+    m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+    _assert_same_model(m, nodes, probs)
+    Xq = X.copy()
+    Xq[:, 1::7] = -FLT_MAX
+    assert np.array_equal(f.predict(Xq), oracle.predict(m, Xq))
+
+
+@pytest.mark.parametrize("n_rows", [1, 2, 3, 33, 4097])
+def test_tiny_and_boundary_sizes(dml, n_rows):
+    X, y = synth.rf_multiclass(n_rows, 5, n_classes=2, n_int=1, seed=n_rows)
+    for algo in (0, 1):
+        kw = dict(algo=algo, n_trees=3, K=2, max_depth=20, min_node_size=1, n_classes=2, seed=1)
+        m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+        _assert_same_model(m, nodes, probs, (n_rows, algo))
+
+
+def test_many_classes(dml):
+    X, y = synth.rf_multiclass(3000, 10, n_classes=32, n_int=2, seed=71)
+    for algo in (0, 1):
+        kw = dict(algo=algo, n_trees=4, K=4, max_depth=12, min_node_size=5, n_classes=32, seed=2)
+        m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+        _assert_same_model(m, nodes, probs, algo)
+        assert np.array_equal(f.predict(X), oracle.predict(m, X))
+
+
+def test_regression_negative_and_tiny_targets(dml):
+    X, _ = synth.rf_regression(1500, 6, seed=81)
+    rng = np.random.default_rng(0)
+    y = (rng.standard_normal(1500) * 1e-3 - 5e-4).astype(np.float32)
+    for algo in (0, 1):
+        kw = dict(algo=algo, task=1, n_trees=4, K=3, max_depth=10, min_node_size=5, seed=2)
+        m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+        _assert_same_model(m, nodes, probs, algo)
+        pg, po = f.predict(X), oracle.predict(m, X)
+        assert np.array_equal(pg, po)
+
+
+def test_invalid_inputs_rejected(dml):
+    X, y = synth.ert_binary(200, 5, seed=1)
+    Xn = X.copy()
+    Xn[1, 3] = np.nan
+    with pytest.raises(dml.DmlError) as e:
+        dml.fit(Xn, y, algo=1, n_trees=2, n_classes=2)
+    assert e.value.status == 1
+    yb = y.copy()
+    yb[0] = 2.0
+    with pytest.raises(dml.DmlError):
+        dml.fit(X, yb, algo=0, n_trees=2, n_classes=2)
+    with pytest.raises(dml.DmlError):
+        dml.fit(X, y, algo=0, n_trees=2, n_classes=64)
+    # the context stays usable after rejected calls
+    f = dml.fit(X, y, algo=1, n_trees=2, n_classes=2)
+    assert f.info().n_trees == 2
+
+
+def test_device_pointers_through_the_c_abi(dml):
+    torch = pytest.importorskip("torch")
+    X, y = synth.ert_binary(1000, 9, seed=91)
+    kw = dict(algo=0, n_trees=5, K=3, max_depth=10, min_node_size=5, n_classes=2, seed=6)
+    fh = dml.fit(X, y, **kw)
+    fd = dml.fit(torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda(), **kw)
+    assert np.array_equal(fh.export()[0], fd.export()[0])
+    out = fd.predict(torch.from_numpy(X).cuda())
+    assert np.array_equal(out.cpu().numpy(), fh.predict(X))
+
+
+def test_import_reference_layout_model(dml):
+    """A model in the kNodeArray/kProbArray layout built elsewhere (here: the
+    oracle) imports and predicts identically."""
+    X, y = synth.ert_binary(800, 10, seed=3)
+    m = oracle.fit(X, y, algo=1, n_trees=9, K=3, max_depth=8, min_node_size=5, n_classes=2,
+                   seed=1)
+    f = dml.Forest.from_model(m.nodes, m.probs, task=0, n_trees=9, n_classes=2, n_features=10)
+    assert np.array_equal(f.predict(X), oracle.predict(m, X))
