@@ -1,0 +1,327 @@
+"""Benchmark: random-forest build on one GB300 (and N independent replicas).
+
+Workload (the headline configuration): RF multiclass with bootstrap,
+1,000,000 rows x 128 FP32 features (N(0,1), 16 of them integers 0..15 stored as
+float), 10 classes, 128 trees, entropy, 11 features tried per node, max depth
+20, min leaf 2 (min node size 5, the reference default).  Seeded synthetic data.
+
+A step is one complete forest fit.  ``value`` is forest-build throughput in
+nodes/s (internal + leaf nodes created per second of device time) with the
+samples already resident in HBM; ``e2e`` is the same metric through the C ABI
+with pinned host buffers (the samples' upload and the model's download inside
+the timed region).  ``--impl reference`` times the reference path's CPU
+restatement on the host cores (the reference itself has no CPU path).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="rf_multiclass_1Mx128_c10_128trees", rows=1_000_000, features=128,
+                classes=10, n_int=16, trees=128, K=11, max_depth=20, min_node_size=5,
+                min_leaf=2, seed=0)
+SMALL = dict(WORKLOAD, name="rf_multiclass_200kx64_c10_32trees", rows=200_000, features=64,
+             trees=32)
+
+
+def fit_kwargs(w):
+    return dict(algo=0, task=0, n_trees=w["trees"], K=w["K"], max_depth=w["max_depth"],
+                min_node_size=w["min_node_size"], min_leaf=w["min_leaf"],
+                n_classes=w["classes"], seed=w["seed"])
+
+
+def make_data(w):
+    from datamininglibs_gb300 import synth
+    return synth.rf_multiclass(w["rows"], w["features"], n_classes=w["classes"],
+                               n_int=w["n_int"], seed=w["seed"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per unit of the search kernels from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "rf_search_kernels_c2.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_entry_try:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(w, X, y, threads, trees):
+    """The oracle (CPU restatement of the reference path) on all host threads,
+    on the full-size data: ``trees`` of the workload's trees (one per thread
+    when trees >= threads, otherwise the nodes of a level spread over threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    kw = fit_kwargs(w)
+    kw["n_trees"] = trees
+    t0 = time.perf_counter()
+    m = oracle.fit(X, y, threads=threads, **kw)
+    dt = time.perf_counter() - t0
+    return {"value": m.nodes.shape[0] / dt, "unit": "nodes/s", "cores": threads,
+            "kind": "port", "sample": "%d of the %d trees on the full %dx%d data (%.1f s)" % (
+                trees, w["trees"], w["rows"], w["features"], dt)}
+
+
+def run_reference(args, w):
+    """The reference path's CPU restatement timed on the host cores; each step
+    builds one tree of the workload with every host thread."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    X, y = make_data(w)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(w, X, y, threads, 1)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(w, X, y, threads, 1))
+    total = time.perf_counter() - t0
+    value = float(np.mean([v["value"] for v in vals]))
+    cb = dict(vals[-1])
+    cb["value"] = value
+    line = {"impl": "reference", "metric": "rf_build_nodes_per_s", "value": value,
+            "unit": "nodes/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * total / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": w["name"], "sample": "one tree per step, all host threads"},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "nodes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, w):
+    import torch
+
+    import datamininglibs_gb300 as dml
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dml.lib()
+    X, y = make_data(w)
+    Xd = torch.from_numpy(X).cuda()
+    yd = torch.from_numpy(y).cuda()
+    kw = fit_kwargs(w)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        dml.fit(Xd, yd, stream=stream, **kw).free()
+    barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    nodes = entries = entry_tries = launches = 0
+    search_ms = loop_ms = 0.0
+    e0.record(stream)
+    for _ in range(args.steps):
+        f = dml.fit(Xd, yd, stream=stream, **kw)
+        st = dml.ensembles.last_fit_stats()
+        nodes += st.nodes
+        entries += st.entries
+        entry_tries += st.entry_tries
+        launches += st.launches
+        search_ms += st.search_ms
+        loop_ms += st.level_loop_ms
+        last_forest = f
+        if _ != args.steps - 1:
+            f.free()
+    e1.record(stream)
+    barrier()
+    clocks = clk.stop()
+    dev_ms = e0.elapsed_time(e1)
+    t_all = torch.tensor([dev_ms, float(nodes)], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        mx = t_all.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        tot = t_all.clone()
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        dev_ms, nodes_all = mx[0].item(), tot[1].item()
+    else:
+        nodes_all = float(nodes)
+    value = nodes_all / (dev_ms / 1000.0)
+
+    # predict throughput with the last forest (rows resident, > L2)
+    pe0 = torch.cuda.Event(enable_timing=True)
+    pe1 = torch.cuda.Event(enable_timing=True)
+    out = torch.empty((w["rows"], w["classes"]), dtype=torch.float32, device="cuda")
+    last_forest.predict(Xd, out=out, stream=stream)
+    torch.cuda.synchronize()
+    pe0.record(stream)
+    for _ in range(3):
+        last_forest.predict(Xd, out=out, stream=stream)
+    pe1.record(stream)
+    torch.cuda.synchronize()
+    predict_rows_per_s = 3 * w["rows"] / (pe0.elapsed_time(pe1) / 1000.0)
+    finfo = last_forest.info()
+    last_forest.free()
+
+    # e2e: the C ABI with pinned host buffers, upload and model download timed
+    Xh = torch.from_numpy(X).pin_memory()
+    yh = torch.from_numpy(y).pin_memory()
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier()
+    t0 = time.perf_counter()
+    e2e_nodes = 0
+    d2h = 0
+    for _ in range(e2e_steps):
+        f = dml.fit(Xh, yh, stream=stream, **kw)
+        nd, pr = f.export()
+        e2e_nodes += nd.shape[0]
+        d2h += nd.nbytes + pr.nbytes
+        f.free()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    h2d = X.nbytes + y.nbytes
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = measured_peak()
+    alg_bytes = 4.0 * entry_tries + 20.0 * entries
+    achieved = alg_bytes / (search_ms / 1000.0) / 1e9 if search_ms > 0 else None
+    tpu = traffic_from_profile()
+    line = {
+        "metric": "rf_build_nodes_per_s", "value": value, "unit": "nodes/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": w["name"], "rows": w["rows"], "features": w["features"],
+                   "classes": w["classes"], "trees": w["trees"], "features_per_node": w["K"],
+                   "max_depth": w["max_depth"], "min_leaf": w["min_leaf"],
+                   "min_node_size": w["min_node_size"],
+                   "l2": "inputs larger than L2 (%.0f MB of samples)" % (X.nbytes / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "trees_per_s": world * args.steps * w["trees"] / (dev_ms / 1000.0),
+        "nodes_per_fit": nodes / args.steps,
+        "predict_rows_per_s": predict_rows_per_s,
+        "forest": {"nodes": finfo.n_nodes, "max_depth": finfo.max_depth},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": (tpu * entry_tries / args.steps / max(1, launches))
+                     if tpu else None,
+                     "kernel": "split search (k_rf_cta, k_warp_nodes)",
+                     "algorithmic_bytes_per_fit": alg_bytes / args.steps,
+                     "peak_kind": peak_kind,
+                     "search_ms_per_fit": search_ms / args.steps,
+                     "level_loop_ms_per_fit": loop_ms / args.steps},
+        "e2e": {"value": e2e_nodes / e2e_s, "unit": "nodes/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h // e2e_steps},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if world == 1 and not args.no_cpu:
+        th = os.cpu_count() or 1
+        line["cpu_baseline"] = cpu_baseline(w, X, y, th, th)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="a reduced workload for quick checks")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    w = SMALL if args.small else WORKLOAD
+    if args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_ours(args, w)
+
+
+if __name__ == "__main__":
+    main()

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdml_gb300.so")
 
-CUDA_SOURCES = ["fit.cu", "predict.cu", "server.cu"]
+CUDA_SOURCES = ["fit.cu", "predict.cu", "server.cu"] + [
+    "search_cw%d.cu" % cw for cw in (1, 2, 4, 5, 8, 16)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -41,7 +42,7 @@ def _compile(src, extra):
 def build(verbose=False, extra=()):
     os.makedirs(BUILD, exist_ok=True)
     srcs = [s for s in CUDA_SOURCES if os.path.exists(os.path.join(CSRC, s))]
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(os.cpu_count() or 4, len(srcs))) as ex:
         results = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
     objs = [o for o, _ in results]
     if verbose:

@@ -1,0 +1,674 @@
+// RF split search for large nodes (more entries than fit a shared-memory
+// sort): one CTA per (node, try) work item on a persistent grid, each with its
+// own global scratch.  The sort is an LSD radix sort (8-bit digits) over tiles
+// of 2048 pairs: each warp loads its 256-pair chunk with eight loads in flight,
+// ranks digits stably with __match_any_sync, and the tile is reordered in
+// shared memory so that every digit's run is written to global memory as one
+// contiguous stretch.  The boundary scan gives each thread 8 consecutive
+// sorted elements (one block scan of packed class counts per 2048 elements).
+// A second kernel applies the try loop (gpurf.cu:177-245) per node and
+// partitions its entries.
+#pragma once
+#include "fit_kernels.cuh"
+#include "warp_rf.cuh"
+
+namespace dml {
+
+constexpr int kBigBlock = 256;
+constexpr int kBigPer = 8;                       // elements per thread
+constexpr int kBigTile = kBigBlock * kBigPer;    // 2048
+constexpr int kBigWarps = kBigBlock / 32;
+
+struct BigSmem {
+  unsigned whist[kBigWarps][256];
+  unsigned tstart[256];
+  unsigned running[256];
+  unsigned red[2 * kBigWarps];
+  uint32_t tk[kBigTile];
+  uint32_t tv[kBigTile];
+  unsigned long long scan64[kBigWarps];
+  unsigned scan32[kBigWarps];
+};
+
+// One LSD pass of pairs (kin, vin) -> (kout, vout) on byte `shift`.
+// Scratch written earlier in the same kernel is read with plain loads (never
+// the read-only cache path).
+static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout,
+                         int m, int shift, BigSmem& S) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  // global digit histogram
+  for (int i = threadIdx.x; i < kBigWarps * 256; i += kBigBlock) (&S.whist[0][0])[i] = 0;
+  __syncthreads();
+  for (int base = 0; base < m; base += kBigTile) {
+    uint32_t d[kBigPer];
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j) {
+      const int i = base + j * kBigBlock + threadIdx.x;
+      d[j] = i < m ? (kin[i] >> shift) & 255u : 256u;
+    }
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j)
+      if (d[j] < 256u) atomicAdd(&S.whist[warp][d[j]], 1u);
+  }
+  __syncthreads();
+  {
+    const int dg = threadIdx.x;  // kBigBlock == 256: one thread per digit
+    unsigned tot = 0;
+    for (int w = 0; w < kBigWarps; ++w) tot += S.whist[w][dg];
+    unsigned total;
+    unsigned ex = block_excl_scan<kBigBlock, unsigned>(tot, &total, S.scan32);
+    S.running[dg] = ex;
+  }
+  __syncthreads();
+  // tiles: stable local sort in shared memory, contiguous run writes
+  for (int base = 0; base < m; base += kBigTile) {
+    const int tn = min(kBigTile, m - base);
+    const int wbeg = warp * 256;
+    uint32_t k[kBigPer], v[kBigPer];
+#pragma unroll
+    for (int r = 0; r < kBigPer; ++r) {
+      const int i = wbeg + r * 32 + lane;
+      k[r] = i < tn ? kin[base + i] : 0u;
+      v[r] = i < tn ? vin[base + i] : 0u;
+    }
+    for (int i = threadIdx.x; i < kBigWarps * 256; i += kBigBlock) (&S.whist[0][0])[i] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kBigPer; ++r) {
+      const int i = wbeg + r * 32 + lane;
+      const bool act = i < tn;
+      const unsigned mask = __ballot_sync(kFull, act);
+      if (act) {
+        const unsigned dg = (k[r] >> shift) & 255u;
+        const unsigned peers = __match_any_sync(mask, dg);
+        if ((peers & lt) == 0) S.whist[warp][dg] += __popc(peers);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    {
+      const int dg = threadIdx.x;
+      unsigned tot = 0;
+      for (int w = 0; w < kBigWarps; ++w) tot += S.whist[w][dg];
+      unsigned total;
+      unsigned ex = block_excl_scan<kBigBlock, unsigned>(tot, &total, S.scan32);
+      S.tstart[dg] = ex;
+      unsigned run = ex;
+      for (int w = 0; w < kBigWarps; ++w) {
+        unsigned h = S.whist[w][dg];
+        S.whist[w][dg] = run;
+        run += h;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kBigPer; ++r) {
+      const int i = wbeg + r * 32 + lane;
+      const bool act = i < tn;
+      const unsigned mask = __ballot_sync(kFull, act);
+      if (act) {
+        const unsigned dg = (k[r] >> shift) & 255u;
+        const unsigned peers = __match_any_sync(mask, dg);
+        const unsigned pos = S.whist[warp][dg] + __popc(peers & lt);
+        S.tk[pos] = k[r];
+        S.tv[pos] = v[r];
+        __syncwarp(mask);
+        if ((peers & lt) == 0) S.whist[warp][dg] += __popc(peers);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < tn; j += kBigBlock) {
+      const uint32_t kk = S.tk[j];
+      const unsigned dg = (kk >> shift) & 255u;
+      const unsigned pos = S.running[dg] + (j - S.tstart[dg]);
+      kout[pos] = kk;
+      vout[pos] = S.tv[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      const int dg = threadIdx.x;
+      const unsigned end = dg == 255 ? (unsigned)tn : S.tstart[dg + 1];
+      S.running[dg] += end - S.tstart[dg];
+    }
+    __syncthreads();
+  }
+}
+
+// Sorts (k, v) of length m; the result ends in (k, v).  Passes whose byte is
+// the same in every key are skipped.
+static __device__ void big_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2, int m,
+                         BigSmem& S) {
+  unsigned o = 0, an = 0xFFFFFFFFu;
+  for (int base = 0; base < m; base += kBigTile) {
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j) {
+      const int i = base + j * kBigBlock + threadIdx.x;
+      if (i < m) {
+        const uint32_t x = k[i];
+        o |= x;
+        an &= x;
+      }
+    }
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    o |= __shfl_xor_sync(kFull, o, s);
+    an &= __shfl_xor_sync(kFull, an, s);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    S.red[2 * (threadIdx.x >> 5)] = o;
+    S.red[2 * (threadIdx.x >> 5) + 1] = an;
+  }
+  __syncthreads();
+  unsigned oo = 0, aa = 0xFFFFFFFFu;
+  for (int w = 0; w < kBigWarps; ++w) {
+    oo |= S.red[2 * w];
+    aa &= S.red[2 * w + 1];
+  }
+  const unsigned diff = oo ^ aa;
+  __syncthreads();
+  bool primary = true;
+  for (int shift = 0; shift < 32; shift += 8) {
+    if (((diff >> shift) & 255u) == 0) continue;
+    if (primary)
+      big_pass(k, v, k2, v2, m, shift, S);
+    else
+      big_pass(k2, v2, k, v, m, shift, S);
+    primary = !primary;
+    __syncthreads();
+  }
+  if (!primary) {
+    for (int i = threadIdx.x; i < m; i += kBigBlock) {
+      k[i] = k2[i];
+      v[i] = v2[i];
+    }
+    __syncthreads();
+  }
+}
+
+struct BigArgs {
+  LevelArgs L;
+  const int* big;          // big node ids
+  int nbig;
+  const int* retry;        // nodes needing optional tries (phase 2)
+  const int* nretry;       // device count
+  int phase;               // 1 mandatory tries, 2 optional tries
+  int tries_per_node;      // slots per node in this phase
+  Cand* cand;              // [node slot][try slot]
+  int* candL;              // [node slot][try slot][Cmax]
+  uint32_t* slot;          // per-CTA scratch: 4 * slot_stride words
+  long long slot_stride;   // >= the largest node's entry count
+  Cand* partial;           // [big index] best of the mandatory tries
+  int* partialL;           // [big index][Cmax]
+  int* retry_out;          // append list of nodes (phase 1 decide)
+  int* nretry_out;
+  int* big_index;          // node id -> index in `big` (for phase 2)
+};
+
+// Boundary scan of a sorted item: each thread owns 8 consecutive elements.
+// Values: classification items carry (label << 27 | weight) through the sort
+// (packed == true); otherwise the value is the entry index into elab/ew/eq.
+template <int CW>
+__device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed, const int* elab,
+                             const int* ew, const long long* eq, int m, const LNode& nd,
+                             const ProbDesc& P, const int* ncnt, const float2* H, ff prior,
+                             unsigned long long* scan64, float* out_g, int* out_p, long long* out_nl,
+                             long long* out_sl, unsigned long long (&outL)[CW]) {
+  const int C = P.C;
+  const int ml = max(1, P.min_leaf);
+  float bg = -FLT_MAX;
+  int bp = -1;
+  long long bnl = 0, bsl = 0;
+  unsigned long long bL[CW];
+  unsigned long long carry[CW];
+  long long carry_n = 0, carry_s = 0;
+#pragma unroll
+  for (int j = 0; j < CW; ++j) {
+    bL[j] = 0;
+    carry[j] = 0;
+  }
+  for (int base = 0; base < m; base += kBigTile) {
+    const int p0 = base + threadIdx.x * kBigPer;
+    uint32_t kk[kBigPer];
+    int lab[kBigPer], w[kBigPer];
+    long long q[kBigPer];
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j) {
+      const int p = p0 + j;
+      if (p < m) {
+        kk[j] = sk[p];
+        const uint32_t vv = sv[p];
+        if (packed) {
+          lab[j] = (int)(vv >> 27);
+          w[j] = (int)(vv & 0x7FFFFFFu);
+          q[j] = 0;
+        } else if (P.task == 0) {
+          const int e = (int)vv;
+          w[j] = ew ? ew[e] : 1;
+          lab[j] = elab[e];
+          q[j] = 0;
+        } else {
+          const int e = (int)vv;
+          w[j] = ew ? ew[e] : 1;
+          lab[j] = -1;
+          q[j] = eq[e];
+        }
+      } else {
+        kk[j] = 0xFFFFFFFFu;
+        w[j] = 0;
+        lab[j] = -1;
+        q[j] = 0;
+      }
+    }
+    const uint32_t prevk0 = p0 > 0 && p0 - 1 < m ? sk[p0 - 1] : 0u;
+    // per-thread totals -> block exclusive scans
+    long long tn = 0, ts = 0;
+    unsigned long long tl[CW];
+#pragma unroll
+    for (int c = 0; c < CW; ++c) tl[c] = 0;
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j) {
+      tn += w[j];
+      if (P.task == 0) {
+#pragma unroll
+        for (int c = 0; c < CW; ++c)
+          tl[c] += (lab[j] == 2 * c ? (unsigned long long)w[j] : 0ull) |
+                   (lab[j] == 2 * c + 1 ? ((unsigned long long)w[j] << 32) : 0ull);
+      } else {
+        ts += q[j] * (long long)w[j];
+      }
+    }
+    unsigned long long tot;
+    long long run_n = carry_n + (long long)block_excl_scan<kBigBlock, unsigned long long>(
+                                    (unsigned long long)tn, &tot, scan64);
+    carry_n += (long long)tot;
+    long long run_s = 0;
+    unsigned long long runL[CW];
+    if (P.task == 0) {
+#pragma unroll
+      for (int c = 0; c < CW; ++c) {
+        runL[c] = carry[c] + block_excl_scan<kBigBlock, unsigned long long>(tl[c], &tot, scan64);
+        carry[c] += tot;
+      }
+    } else {
+      run_s = carry_s + (long long)block_excl_scan<kBigBlock, unsigned long long>(
+                            (unsigned long long)ts, &tot, scan64);
+      carry_s += (long long)tot;
+#pragma unroll
+      for (int c = 0; c < CW; ++c) runL[c] = 0;
+    }
+    uint32_t prevk = prevk0;
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j) {
+      const int p = p0 + j;
+      if (p < m && p > 0 && prevk < kk[j]) {
+        const long long nr = (long long)nd.n - run_n;
+        if (run_n >= ml && nr >= ml) {
+          float g;
+          if (P.task == 0)
+            g = entropy_gain(
+                H, prior, C, run_n, nr, [&](int c) { return packed_get<CW>(runL, c); },
+                [&](int c) { return (long long)ncnt[c]; });
+          else
+            g = variance_gain(run_n, run_s, nr, nd.sum - run_s, P.S);
+          if (bp < 0 || g > bg) {
+            bg = g;
+            bp = p;
+            bnl = run_n;
+            bsl = run_s;
+#pragma unroll
+            for (int c = 0; c < CW; ++c) bL[c] = runL[c];
+          }
+        }
+      }
+      prevk = kk[j];
+      run_n += w[j];
+      if (P.task == 0) {
+#pragma unroll
+        for (int c = 0; c < CW; ++c)
+          runL[c] += (lab[j] == 2 * c ? (unsigned long long)w[j] : 0ull) |
+                     (lab[j] == 2 * c + 1 ? ((unsigned long long)w[j] << 32) : 0ull);
+      } else {
+        run_s += q[j] * (long long)w[j];
+      }
+    }
+  }
+  *out_g = bg;
+  *out_p = bp;
+  *out_nl = bnl;
+  *out_sl = bsl;
+#pragma unroll
+  for (int c = 0; c < CW; ++c) outL[c] = bL[c];
+}
+
+template <int CW>
+__global__ void __launch_bounds__(kBigBlock) k_rf_big_items(BigArgs b) {
+  __shared__ BigSmem S;
+  __shared__ float s_g[kBigBlock];
+  __shared__ int s_p[kBigBlock];
+  __shared__ ff s_prior;
+  const LevelArgs& a = b.L;
+  const int nnodes = b.phase == 1 ? b.nbig : *b.nretry;
+  const long long nitems = (long long)nnodes * b.tries_per_node;
+  uint32_t* k1 = b.slot + (long long)blockIdx.x * 4 * b.slot_stride;
+  uint32_t* v1 = k1 + b.slot_stride;
+  uint32_t* k2 = v1 + b.slot_stride;
+  uint32_t* v2 = k2 + b.slot_stride;
+  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int ni = (int)(it / b.tries_per_node);
+    const int ts = (int)(it % b.tries_per_node);
+    const int node = b.phase == 1 ? b.big[ni] : b.retry[ni];
+    const LNode nd = a.nodes[node];
+    const ProbDesc& P = a.probs[nd.prob];
+    const int t = b.phase == 1 ? ts : P.n_mand + ts;
+    const int slot_node = b.phase == 1 ? ni : b.big_index[node];
+    Cand* cout = b.cand + (long long)slot_node * kMaxTries + t;
+    if ((b.phase == 1 && ts >= P.n_mand) || (b.phase == 2 && ts >= P.n_opt)) continue;
+    const int m = nd.ecnt;
+    const int* rows = a.rowsA + nd.ebeg;
+    const int* ncnt = a.cnt + (long long)node * a.Cmax;
+    const int f = feature_of_try(P, nd, t);
+    const float* xf = P.X + (long long)f * P.N;
+    if (threadIdx.x == 0 && P.task == 0)
+      s_prior = entropy_prior(a.H, nd.n, P.C, [&](int c) { return (long long)ncnt[c]; });
+    // keys (and, for classification, the packed label | weight values) with
+    // eight gathers in flight per thread
+    const bool packed = P.task == 0;
+    const int* wts = a.wA ? a.wA + nd.ebeg : nullptr;
+    for (int base = 0; base < m; base += kBigTile) {
+      int rr[kBigPer];
+#pragma unroll
+      for (int j = 0; j < kBigPer; ++j) {
+        const int i = base + j * kBigBlock + threadIdx.x;
+        rr[j] = i < m ? __ldg(rows + i) : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < kBigPer; ++j) {
+        const int i = base + j * kBigBlock + threadIdx.x;
+        if (i < m) {
+          k1[i] = orderable(__ldg(xf + rr[j]));
+          v1[i] = packed ? ((uint32_t)__ldg(P.lab + rr[j]) << 27) |
+                               (uint32_t)(wts ? __ldg(wts + i) : 1)
+                         : (uint32_t)i;
+        }
+      }
+    }
+    __syncthreads();
+    big_sort(k1, v1, k2, v2, m, S);
+    // regression: per-entry targets in the free second buffer
+    long long* eq = (long long*)k2;  // k2, v2 contiguous: 8 bytes per entry
+    if (!packed) {
+      for (int i = threadIdx.x; i < m; i += kBigBlock) eq[i] = __ldg(P.q + __ldg(rows + i));
+      __syncthreads();
+    }
+    float g;
+    int p;
+    long long nl, sl;
+    unsigned long long L[CW];
+    big_boundary<CW>(k1, v1, packed, nullptr, wts, eq, m, nd, P, ncnt, a.H, s_prior, S.scan64, &g,
+                     &p, &nl, &sl, L);
+    s_g[threadIdx.x] = g;
+    s_p[threadIdx.x] = p;
+    __syncthreads();
+    for (int s = kBigBlock / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        const float g2 = s_g[threadIdx.x + s];
+        const int p2 = s_p[threadIdx.x + s];
+        const float g1 = s_g[threadIdx.x];
+        const int p1 = s_p[threadIdx.x];
+        if (p2 >= 0 && (p1 < 0 || g2 > g1 || (g2 == g1 && p2 < p1))) {
+          s_g[threadIdx.x] = g2;
+          s_p[threadIdx.x] = p2;
+        }
+      }
+      __syncthreads();
+    }
+    const int bp = s_p[0];
+    if (bp >= 0 && p == bp) {
+      Cand c;
+      c.valid = 1;
+      c.gain = g;
+      c.f = f;
+      // the values on both sides of the boundary (-0 reads back as +0, which
+      // gives the same threshold)
+      const float xa = packed ? from_orderable(k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
+      const float xb = packed ? from_orderable(k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
+      c.thr = midpoint_threshold(xa, xb);
+      c.nl_e = bp;
+      c.nl = (int)nl;
+      c.suml = sl;
+      *cout = c;
+      if (P.task == 0) {
+        int* lo = b.candL + ((long long)slot_node * kMaxTries + t) * a.Cmax;
+        for (int cc = 0; cc < P.C; ++cc) lo[cc] = (int)packed_get<CW>(L, cc);
+      }
+    }
+    if (bp < 0 && threadIdx.x == 0) {
+      Cand c;
+      c.valid = 0;
+      c.gain = -FLT_MAX;
+      c.f = f;
+      c.thr = 0.0f;
+      c.nl_e = c.nl = 0;
+      c.suml = 0;
+      *cout = c;
+    }
+    if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)m);
+    __syncthreads();
+  }
+}
+
+// Try loop per big node.  Phase 1: best of the mandatory tries; nodes whose
+// best is not sensible (and that have optional tries) go to the retry list,
+// the others are decided.  Phase 2: optional tries in order until one is
+// sensible.  Decided nodes write their result and partition their entries.
+template <int CW>
+__global__ void __launch_bounds__(kBigBlock) k_rf_big_decide(BigArgs b) {
+  __shared__ Cand s_best;
+  __shared__ int s_bestL[kMaxClasses];
+  __shared__ int s_act;
+  __shared__ int s_scan[kBigWarps];
+  const LevelArgs& a = b.L;
+  const int nnodes = b.phase == 1 ? b.nbig : *b.nretry;
+  for (int ni = blockIdx.x; ni < nnodes; ni += gridDim.x) {
+    const int node = b.phase == 1 ? b.big[ni] : b.retry[ni];
+    const int bi = b.phase == 1 ? ni : b.big_index[node];
+    const LNode nd = a.nodes[node];
+    const ProbDesc& P = a.probs[nd.prob];
+    const Cand* cs = b.cand + (long long)bi * kMaxTries;
+    const int* cL = b.candL + (long long)bi * kMaxTries * a.Cmax;
+    if (threadIdx.x == 0) {
+      int from = -1;
+      if (b.phase == 1) {
+        Cand best = cs[0];
+        from = 0;
+        for (int t = 1; t < P.n_mand; ++t)
+          if (better(cs[t], best)) {
+            best = cs[t];
+            from = t;
+          }
+        b.big_index[node] = ni;
+        if (P.n_opt > 0 && !(best.valid && best.gain >= kSensible)) {
+          b.partial[ni] = best;
+          for (int c = 0; c < P.C; ++c)
+            b.partialL[(long long)ni * a.Cmax + c] = P.task == 0 ? cL[from * a.Cmax + c] : 0;
+          b.retry_out[atomicAdd(b.nretry_out, 1)] = node;
+          s_act = 0;
+        } else {
+          s_best = best;
+          if (P.task == 0)
+            for (int c = 0; c < P.C; ++c) s_bestL[c] = cL[from * a.Cmax + c];
+          s_act = 1;
+        }
+      } else {
+        Cand best = b.partial[bi];
+        const int* pl = b.partialL + (long long)bi * a.Cmax;
+        int bestL_src = -1;
+        for (int j = 0; j < P.n_opt; ++j) {
+          const Cand& c = cs[P.n_mand + j];
+          if (better(c, best)) {
+            best = c;
+            bestL_src = P.n_mand + j;
+          }
+          if (c.valid && c.gain >= kSensible) break;
+        }
+        s_best = best;
+        if (P.task == 0)
+          for (int c = 0; c < P.C; ++c)
+            s_bestL[c] = bestL_src < 0 ? pl[c] : cL[bestL_src * a.Cmax + c];
+        s_act = 1;
+      }
+    }
+    __syncthreads();
+    if (s_act) {
+      const Cand bb = s_best;
+      if (!bb.valid) {
+        if (threadIdx.x == 0) write_leaf(a.res, node);
+      } else {
+        if (threadIdx.x == 0)
+          write_result(a.res, a.res_cnt, a.Cmax, node, bb, P.task == 0 ? s_bestL : nullptr, P.C);
+        cta_partition<kBigBlock>(a.rowsA, a.wA, a.rowsB, a.wB, nd.ebeg, nd.ecnt, bb.nl_e,
+                                 P.X + (long long)bb.f * P.N, bb.thr, s_scan);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// RF node of 257 .. SMEM_CAP entries in one CTA: keys and values sorted in
+// shared memory, then the same 8-per-thread boundary scan as the large path.
+template <int CW, int SMEM_CAP>
+__global__ void __launch_bounds__(kBigBlock) k_rf_smem(LevelArgs a) {
+  __shared__ SortSmem<kBigBlock> SS;
+  __shared__ unsigned red[2 * kBigWarps];
+  __shared__ unsigned long long scan64[kBigWarps];
+  __shared__ float s_g[kBigBlock];
+  __shared__ int s_p[kBigBlock];
+  __shared__ Cand s_cand, s_best;
+  __shared__ int s_candL[kMaxClasses], s_bestL[kMaxClasses];
+  __shared__ ff s_prior;
+  __shared__ int s_scan[kBigWarps];
+  __shared__ int s_next;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  uint32_t* k1 = (uint32_t*)dsm;
+  uint32_t* v1 = k1 + SMEM_CAP;
+  uint32_t* k2 = k1 + 2 * SMEM_CAP;
+  uint32_t* v2 = k1 + 3 * SMEM_CAP;
+  long long* q_e = (long long*)(k1 + 4 * SMEM_CAP);
+  for (int wi = blockIdx.x; wi < a.nwork; wi += gridDim.x) {
+    const int node = a.work[wi];
+    const LNode nd = a.nodes[node];
+    const ProbDesc& P = a.probs[nd.prob];
+    const int C = P.C;
+    const int m = nd.ecnt;
+    const int* rows = a.rowsA + nd.ebeg;
+    const int* wts = a.wA ? a.wA + nd.ebeg : nullptr;
+    const int* ncnt = a.cnt + (long long)node * a.Cmax;
+    const bool packed = P.task == 0;
+    if (!packed)
+      for (int i = threadIdx.x; i < m; i += kBigBlock) q_e[i] = __ldg(P.q + __ldg(rows + i));
+    if (threadIdx.x == 0 && packed)
+      s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
+    __syncthreads();
+    int t = 0;
+    while (true) {
+      const int f = feature_of_try(P, nd, t);
+      const float* xf = P.X + (long long)f * P.N;
+      for (int i = threadIdx.x; i < m; i += kBigBlock) {
+        const int row = __ldg(rows + i);
+        k1[i] = orderable(__ldg(xf + row));
+        v1[i] = packed ? ((uint32_t)__ldg(P.lab + row) << 27) | (uint32_t)(wts ? __ldg(wts + i) : 1)
+                       : (uint32_t)i;
+      }
+      __syncthreads();
+      cta_radix_sort<kBigBlock>(k1, v1, k2, v2, m, SS, red);
+      float g;
+      int p;
+      long long nl, sl;
+      unsigned long long L[CW];
+      big_boundary<CW>(k1, v1, packed, nullptr, wts, q_e, m, nd, P, ncnt, a.H, s_prior, scan64,
+                       &g, &p, &nl, &sl, L);
+      s_g[threadIdx.x] = g;
+      s_p[threadIdx.x] = p;
+      __syncthreads();
+      for (int st = kBigBlock / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+          const float g2 = s_g[threadIdx.x + st];
+          const int p2 = s_p[threadIdx.x + st];
+          const float g1 = s_g[threadIdx.x];
+          const int p1 = s_p[threadIdx.x];
+          if (p2 >= 0 && (p1 < 0 || g2 > g1 || (g2 == g1 && p2 < p1))) {
+            s_g[threadIdx.x] = g2;
+            s_p[threadIdx.x] = p2;
+          }
+        }
+        __syncthreads();
+      }
+      const int bp = s_p[0];
+      if (bp >= 0 && p == bp) {
+        Cand c;
+        c.valid = 1;
+        c.gain = g;
+        c.f = f;
+        const float xa = packed ? from_orderable(k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
+        const float xb = packed ? from_orderable(k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
+        c.thr = midpoint_threshold(xa, xb);
+        c.nl_e = bp;
+        c.nl = (int)nl;
+        c.suml = sl;
+        s_cand = c;
+        if (packed)
+          for (int cc = 0; cc < C; ++cc) s_candL[cc] = (int)packed_get<CW>(L, cc);
+      }
+      if (bp < 0 && threadIdx.x == 0) {
+        Cand c;
+        c.valid = 0;
+        c.gain = -FLT_MAX;
+        c.f = f;
+        c.thr = 0.0f;
+        c.nl_e = c.nl = 0;
+        c.suml = 0;
+        s_cand = c;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        bool next;
+        if (t < P.n_mand) {
+          if (t == 0 || better(s_cand, s_best)) {
+            s_best = s_cand;
+            if (packed)
+              for (int c = 0; c < C; ++c) s_bestL[c] = s_candL[c];
+          }
+          next = (t + 1 < P.n_mand) || (P.n_opt > 0 && !(s_best.valid && s_best.gain >= kSensible));
+        } else {
+          if (better(s_cand, s_best)) {
+            s_best = s_cand;
+            if (packed)
+              for (int c = 0; c < C; ++c) s_bestL[c] = s_candL[c];
+          }
+          next = !(s_cand.valid && s_cand.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
+        }
+        s_next = next ? 1 : 0;
+      }
+      __syncthreads();
+      const bool stop = s_next == 0;
+      __syncthreads();
+      ++t;
+      if (stop) break;
+    }
+    const Cand b = s_best;
+    if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)t * m);
+    if (!b.valid) {
+      if (threadIdx.x == 0) write_leaf(a.res, node);
+    } else {
+      if (threadIdx.x == 0)
+        write_result(a.res, a.res_cnt, a.Cmax, node, b, packed ? s_bestL : nullptr, C);
+      cta_partition<kBigBlock>(a.rowsA, a.wA, a.rowsB, a.wB, nd.ebeg, m, b.nl_e,
+                               P.X + (long long)b.f * P.N, b.thr, s_scan);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace dml

@@ -10,12 +10,14 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
 
 #include "engine.h"
 #include "level_kernels.cuh"
+#include "search_launch.cuh"
 
 namespace dml {
 
@@ -134,8 +136,6 @@ struct DBuf {
   }
 };
 
-constexpr int kBlock = 256;
-constexpr int kSmemCap = 4096;    // RF nodes up to this many entries sort in shared memory
 constexpr int kPlainChunk = 512;  // reference: max_blocks_ / max_nominal_ nodes per launch
 
 // n*ln(n) table cached on the device across fits (grow-only).
@@ -163,30 +163,26 @@ static const float2* nlogn_table(long long nmax, cudaStream_t s) {
 }
 
 template <int CW>
-static void set_smem_attrs() {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    cudaFuncSetAttribute(k_rf_cta<kBlock, CW, kSmemCap>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemCap * 24);
-  });
-}
-
+void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s);
+extern template void launch_search_cw<1>(int, const LevelArgs&, int, cudaStream_t);
+extern template void launch_search_cw<2>(int, const LevelArgs&, int, cudaStream_t);
+extern template void launch_search_cw<4>(int, const LevelArgs&, int, cudaStream_t);
+extern template void launch_search_cw<5>(int, const LevelArgs&, int, cudaStream_t);
+extern template void launch_search_cw<8>(int, const LevelArgs&, int, cudaStream_t);
+extern template void launch_search_cw<16>(int, const LevelArgs&, int, cudaStream_t);
 template <int CW>
-static void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s) {
-  LevelArgs b = a;
-  b.nwork = count;
-  if (q == kQWarp) {
-    int blocks = std::max(1, std::min((count + 7) / 8, 1 << 20));
-    k_warp_nodes<CW><<<blocks, 256, 0, s>>>(b);
-  } else if (q == kQErt) {
-    k_ert_cta<kBlock><<<std::min(count, 1 << 20), kBlock, 0, s>>>(b);
-  } else {
-    set_smem_attrs<CW>();
-    size_t dsm = q == kQRfSmall ? (size_t)kSmemCap * 24 : 0;
-    k_rf_cta<kBlock, CW, kSmemCap><<<std::min(count, 1 << 20), kBlock, dsm, s>>>(
-        b, q == kQRfBig ? 1 : 0);
+void launch_big_cw(BigArgs b, int phase, int grid, int decide_grid, int tries, cudaStream_t s);
+
+static void launch_big(int CW, const BigArgs& b, int phase, int grid, int dgrid, int tries,
+                       cudaStream_t s) {
+  switch (CW) {
+    case 1: launch_big_cw<1>(b, phase, grid, dgrid, tries, s); break;
+    case 2: launch_big_cw<2>(b, phase, grid, dgrid, tries, s); break;
+    case 4: launch_big_cw<4>(b, phase, grid, dgrid, tries, s); break;
+    case 5: launch_big_cw<5>(b, phase, grid, dgrid, tries, s); break;
+    case 8: launch_big_cw<8>(b, phase, grid, dgrid, tries, s); break;
+    default: launch_big_cw<16>(b, phase, grid, dgrid, tries, s); break;
   }
-  DML_CK(cudaGetLastError());
 }
 
 static void launch_search(int CW, int q, const LevelArgs& a, int count, cudaStream_t s) {
@@ -194,6 +190,7 @@ static void launch_search(int CW, int q, const LevelArgs& a, int count, cudaStre
     case 1: launch_search_cw<1>(q, a, count, s); break;
     case 2: launch_search_cw<2>(q, a, count, s); break;
     case 4: launch_search_cw<4>(q, a, count, s); break;
+    case 5: launch_search_cw<5>(q, a, count, s); break;
     case 8: launch_search_cw<8>(q, a, count, s); break;
     default: launch_search_cw<16>(q, a, count, s); break;
   }
@@ -238,7 +235,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       set_error("forest %d: n_trees, n_rows and n_features must be positive, data non-null", i);
       throw InvalidArg{};
     }
-    if (d.n_rows >= (1ll << 30) || (long long)d.n_rows * d.n_features >= (1ll << 40)) {
+    // RF classification packs (label, bootstrap weight <= n_rows) into 32 bits
+    if (d.n_rows >= (1ll << 27) || (long long)d.n_rows * d.n_features >= (1ll << 40)) {
       set_error("forest %d: too many rows", i);
       throw InvalidArg{};
     }
@@ -282,7 +280,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     if (d.algo == DML_ALGO_RF) any_weights = true;
     if (d.task == DML_CLASSIFICATION) H_n = std::max(H_n, (long long)d.n_rows);
   }
-  const int CW = Cmax <= 2 ? 1 : Cmax <= 4 ? 2 : Cmax <= 8 ? 4 : Cmax <= 16 ? 8 : 16;
+  const int CW = Cmax <= 2 ? 1 : Cmax <= 4 ? 2 : Cmax <= 8 ? 4 : Cmax <= 10 ? 5 : Cmax <= 16 ? 8 : 16;
   dml_fit_stats st;
   std::memset(&st, 0, sizeof(st));
 
@@ -300,6 +298,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
   DBuf<ClassifyNode> node_log;
   DBuf<float> prob_log;
   DBuf<Seg> segs;
+  DBuf<Cand> big_cand, big_partial;
+  DBuf<int> big_candL, big_partialL, big_retry, big_index;
   std::vector<dml_forest*> forests;
   auto release_all = [&]() {
     for (void* p : owned) dev_free(p, s);
@@ -318,6 +318,12 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     node_log.release(s);
     prob_log.release(s);
     segs.release(s);
+    big_cand.release(s);
+    big_partial.release(s);
+    big_candL.release(s);
+    big_partialL.release(s);
+    big_retry.release(s);
+    big_index.release(s);
   };
   try {
     // ---------------------------------------------------- data to device
@@ -344,6 +350,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       int grid = (int)std::min<long long>(4096, (nx + 255) / 256);
       k_validate<<<grid, 256, 0, s>>>(H.X, nx, H.y, P.N, P.task, P.C, d_err, d_max + i);
       DML_CK(cudaGetLastError());
+      ++st.launches;
       if (P.task == 0)
         H.lab = (int*)alloc(sizeof(int) * P.N);
       else
@@ -377,6 +384,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       int grid = (int)std::min<long long>(4096, (P.N + 255) / 256);
       k_prep_targets<<<grid, 256, 0, s>>>(ph[i].y, P.N, P.task, P.S, ph[i].lab, ph[i].q);
       DML_CK(cudaGetLastError());
+      ++st.launches;
     }
     const float2* H = H_n > 0 ? nlogn_table(H_n, s) : nullptr;
 
@@ -386,6 +394,24 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     int* wA = any_weights ? (int*)alloc(sizeof(int) * total_slots) : nullptr;
     int* wB = any_weights ? (int*)alloc(sizeof(int) * total_slots) : nullptr;
     uint2* scratch = any_weights ? (uint2*)alloc(sizeof(uint2) * 2 * total_slots) : nullptr;
+    // big-node scratch: 4 words per entry of the largest RF tree, per CTA
+    int max_mand = 1, max_opt = 0;
+    long long slot_stride = 0;
+    for (auto& P : hp) {
+      max_mand = std::max(max_mand, P.n_mand);
+      max_opt = std::max(max_opt, P.n_opt);
+      if (P.algo == DML_ALGO_RF && P.N > kSmemCap) slot_stride = std::max(slot_stride, P.N);
+    }
+    int sms = 148;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int big_grid = 2 * sms;
+    if (slot_stride > 0) {
+      const long long budget = 16ll << 30;
+      big_grid = (int)std::max(1ll, std::min<long long>(big_grid, budget / (16 * slot_stride)));
+    }
+    uint32_t* big_slot =
+        slot_stride > 0 ? (uint32_t*)alloc(sizeof(uint32_t) * 4 * slot_stride * big_grid) : nullptr;
+    int* d_nretry = (int*)alloc(sizeof(int));
     ProbDesc* d_probs = (ProbDesc*)alloc(sizeof(ProbDesc) * nprob);
     DML_CK(cudaMemcpyAsync(d_probs, hp.data(), sizeof(ProbDesc) * nprob, cudaMemcpyHostToDevice, s));
     std::vector<int> tree_prob(total_trees);
@@ -404,8 +430,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     }
     int* d_qcount = (int*)alloc(sizeof(int) * kNumQ);
     int* d_summary = (int*)alloc(sizeof(int) * 2);
-    long long* d_stats = (long long*)alloc(sizeof(long long) * 2);
-    DML_CK(cudaMemsetAsync(d_stats, 0, sizeof(long long) * 2, s));
+    long long* d_stats = (long long*)alloc(sizeof(long long) * 4);
+    DML_CK(cudaMemsetAsync(d_stats, 0, sizeof(long long) * 4, s));
     Summary* h_sum = nullptr;
     DML_CK(cudaMallocHost(&h_sum, sizeof(Summary)));
 
@@ -439,7 +465,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       ++st.launches;
     }
     k_roots<1024><<<total_trees, 1024, 0, s>>>(d_probs, d_tree_prob, (const int*)scratch, rowsA,
-                                               wA, cur.p, cnt_cur.p, Cmax, res_cur.p, queues());
+                                               wA, cur.p, cnt_cur.p, Cmax, res_cur.p, queues(),
+                                               d_stats);
     DML_CK(cudaGetLastError());
     ++st.launches;
     DML_CK(cudaMemcpyAsync(h_sum->qcount, d_qcount, sizeof(int) * kNumQ, cudaMemcpyDeviceToHost, s));
@@ -448,9 +475,13 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     long long log_base = 0, plog_base = 0;
     int depth = 0;
     float search_ms_total = 0.0f;
-    cudaEvent_t es0, es1;
+    cudaEvent_t es0, es1, tq0, tq1;
     DML_CK(cudaEventCreate(&es0));
     DML_CK(cudaEventCreate(&es1));
+    DML_CK(cudaEventCreate(&tq0));
+    DML_CK(cudaEventCreate(&tq1));
+    const char* tenv = getenv("DML_TRACE");
+    const bool trace = tenv && tenv[0] == '1';
     while (n > 0) {
       // ------------------------------------------- search + partition
       LevelArgs a;
@@ -468,14 +499,65 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       a.scratch = scratch;
       a.scratch_half = total_slots;
       a.H = H;
+      a.stats = d_stats;
       int qc[kNumQ];
       std::memcpy(qc, h_sum->qcount, sizeof(qc));
       DML_CK(cudaEventRecord(es0, s));
+      float qms[kNumQ] = {0, 0, 0, 0, 0, 0, 0, 0};
       for (int q = 0; q < kNumQ; ++q) {
         if (qc[q] <= 0) continue;
+        if (q == kQRfBig) {
+          // per-(node, try) items on a persistent grid with per-CTA scratch
+          const int nb = qc[q];
+          big_cand.reserve((size_t)nb * kMaxTries, s, false);
+          big_candL.reserve((size_t)nb * kMaxTries * Cmax, s, false);
+          big_partial.reserve((size_t)nb, s, false);
+          big_partialL.reserve((size_t)nb * Cmax, s, false);
+          big_retry.reserve((size_t)nb, s, false);
+          big_index.reserve((size_t)n, s, false);
+          BigArgs b;
+          b.L = a;
+          b.big = qlist[q].p;
+          b.nbig = nb;
+          b.retry = big_retry.p;
+          b.nretry = d_nretry;
+          b.cand = big_cand.p;
+          b.candL = big_candL.p;
+          b.slot = big_slot;
+          b.slot_stride = slot_stride;
+          b.partial = big_partial.p;
+          b.partialL = big_partialL.p;
+          b.retry_out = big_retry.p;
+          b.nretry_out = d_nretry;
+          b.big_index = big_index.p;
+          DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
+          if (trace) DML_CK(cudaEventRecord(tq0, s));
+          const int chunk = plain ? kPlainChunk : nb;
+          for (int off = 0; off < nb; off += chunk) {
+            b.big = qlist[q].p + off;
+            b.nbig = std::min(chunk, nb - off);
+            DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
+            launch_big(CW, b, 1, big_grid, std::min(b.nbig, 65535), max_mand, s);
+            launch_big(CW, b, 2, big_grid, std::min(b.nbig, 65535), std::max(1, max_opt), s);
+            st.launches += 4;
+            if (plain) DML_CK(cudaStreamSynchronize(s));
+          }
+          if (trace) {
+            DML_CK(cudaEventRecord(tq1, s));
+            DML_CK(cudaEventSynchronize(tq1));
+            cudaEventElapsedTime(&qms[q], tq0, tq1);
+          }
+          continue;
+        }
         if (!plain) {
           a.work = qlist[q].p;
+          if (trace) DML_CK(cudaEventRecord(tq0, s));
           launch_search(CW, q, a, qc[q], s);
+          if (trace) {
+            DML_CK(cudaEventRecord(tq1, s));
+            DML_CK(cudaEventSynchronize(tq1));
+            cudaEventElapsedTime(&qms[q], tq0, tq1);
+          }
           ++st.launches;
         } else {
           for (int off = 0; off < qc[q]; off += kPlainChunk) {
@@ -546,6 +628,13 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       float sm = 0.0f;
       cudaEventElapsedTime(&sm, es0, es1);
       search_ms_total += sm;
+      if (trace)
+        fprintf(stderr,
+                "[dml] level %2d nodes %9d | w32 %8d %7.2f | ert %6d %7.2f | w64 %7d %7.2f | w128 %7d "
+                "%7.2f | w256 %7d %7.2f | w512 %7d %7.2f | cta %7d %7.2f | big %5d %7.2f | search "
+                "%8.2f ms\n",
+                depth, n, qc[0], qms[0], qc[1], qms[1], qc[4], qms[4], qc[5], qms[5], qc[6],
+                qms[6], qc[7], qms[7], qc[2], qms[2], qc[3], qms[3], sm);
       log_base += n;
       plog_base += h_sum->leaves;
       n = h_sum->children;
@@ -564,12 +653,15 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     cudaEventDestroy(ev1);
     cudaEventDestroy(es0);
     cudaEventDestroy(es1);
-    long long h_stats[2];
+    cudaEventDestroy(tq0);
+    cudaEventDestroy(tq1);
+    long long h_stats[4];
     DML_CK(cudaMemcpy(h_stats, d_stats, sizeof(h_stats), cudaMemcpyDeviceToHost));
     cudaFreeHost(h_sum);
     st.nodes = log_base;
     st.entries = h_stats[0];
     st.weighted_rows = h_stats[1];
+    st.entry_tries = h_stats[2];
     st.levels = depth;
     st.level_loop_ms = loop_ms;
     st.search_ms = search_ms_total;
@@ -612,12 +704,14 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           f->max_depth = d;
           k_gather_nodes<<<(sg.node_cnt + 255) / 256, 256, 0, s>>>(node_log.p, sg.node_pos,
                                                                    sg.node_cnt, f->nodes + no);
+          ++st.launches;
           no += sg.node_cnt;
           if (sg.leaf_cnt > 0) {
             long long tot = sg.leaf_cnt * hp[i].C;
             int g = (int)std::min<long long>(4096, (tot + 255) / 256);
             k_gather_probs<<<g, 256, 0, s>>>(prob_log.p, sg.leaf_rank, sg.leaf_cnt, Cmax,
                                              hp[i].C, f->probs + po);
+            ++st.launches;
             po += tot;
           }
         }
@@ -625,6 +719,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       }
       dml_status ps = forest_build_pnodes(f, s);
       if (ps != DML_OK) throw CudaError{cudaErrorUnknown};
+      ++st.launches;
     }
     DML_CK(cudaStreamSynchronize(s));
     release_all();

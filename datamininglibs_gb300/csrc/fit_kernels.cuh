@@ -182,6 +182,7 @@ struct LevelArgs {
   uint2* scratch;       // two pair buffers per entry slot: scratch[slot], scratch[slot + total]
   long long scratch_half;
   const float2* H;      // n*ln(n) table
+  long long* stats;     // [2] += tries evaluated x node entries
 };
 
 // ================================================================== ERT (CTA)
@@ -217,10 +218,11 @@ __global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
     if (threadIdx.x == 0 && P.task == 0)
       s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     // chunks: mandatory tries [0, n_mand) in chunks, then one optional chunk
-    int t0 = 0;
+    int t0 = 0, tries_done = 0;
     bool optional = false;
     while (true) {
       const int tcount = optional ? P.n_opt : min(kErtChunk, P.n_mand - t0);
+      tries_done += tcount;
       if (threadIdx.x < tcount) {
         int t = t0 + threadIdx.x;
         int f = feature_of_try(P, nd, t);
@@ -350,6 +352,9 @@ __global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
       }
     }
     const Cand b = s_best;
+    if (threadIdx.x == 0)
+      atomicAdd((unsigned long long*)&a.stats[2],
+                (unsigned long long)tries_done * nd.ecnt);
     if (!b.valid) {
       if (threadIdx.x == 0) write_leaf(a.res, node);
     } else {
@@ -731,6 +736,7 @@ __global__ void __launch_bounds__(BLOCK) k_rf_cta(LevelArgs a, int big) {
       ++t;
     }
     const Cand b = s_best;
+    if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)t * m);
     if (!b.valid) {
       if (threadIdx.x == 0) write_leaf(a.res, node);
     } else {

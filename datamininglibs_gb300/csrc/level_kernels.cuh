@@ -1,6 +1,7 @@
 // Tiny-node warp kernel, root construction, level scans and model emission.
 #pragma once
 #include "fit_kernels.cuh"
+#include "warp_rf.cuh"
 
 namespace dml {
 
@@ -181,7 +182,10 @@ __global__ void __launch_bounds__(256) k_warp_nodes(LevelArgs a) {
         }
         more = !(cd.valid && cd.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
       }
-      if (!more) break;
+      if (!more) {
+        if (lane == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)(t + 1) * m);
+        break;
+      }
     }
     if (!best.valid) {
       if (lane == 0) write_leaf(a.res, node);
@@ -206,7 +210,8 @@ __global__ void __launch_bounds__(256) k_warp_nodes(LevelArgs a) {
 // Node classes: tiny (<= 32 entries, warp), ERT (CTA), RF small (CTA, shared
 // memory sort), RF big (CTA, global sort).  Queue order does not affect
 // results, only scheduling.
-enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kNumQ = 4 };
+enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kQRfW2 = 4, kQRfW4 = 5, kQRfW8 = 6,
+       kQRfW16 = 7, kNumQ = 8 };
 
 struct Queues {
   int* list[kNumQ];
@@ -232,6 +237,9 @@ __device__ __forceinline__ void enqueue(Queues Q, int q, int node, bool want) {
 __device__ __forceinline__ int queue_of(const ProbDesc& P, int ecnt, int small_cap) {
   if (ecnt <= 32) return kQWarp;
   if (P.algo == 1) return kQErt;
+  if (ecnt <= 64) return kQRfW2;
+  if (ecnt <= 128) return kQRfW4;
+  if (ecnt <= 256) return kQRfW8;
   return ecnt <= small_cap ? kQRfSmall : kQRfBig;
 }
 
@@ -239,6 +247,7 @@ __device__ __forceinline__ bool preleaf(const ProbDesc& P, int n, int depth) {
   return n <= P.min_node_size || depth >= P.max_depth;
 }
 
+#ifndef DML_SEARCH_CW  // driver-only kernels (fit.cu)
 // ============================================================ roots
 // RF bootstrap multiplicities: row r of tree t is drawn w[r] times among the
 // N draws keyed (seed, tree, i) (gpurf.cu:101-113 with keyed draws).
@@ -264,7 +273,7 @@ template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_roots(const ProbDesc* probs, const int* tree_prob,
                                                  const int* wcnt, int* rows, int* wts,
                                                  LNode* nodes, int* cnt, int Cmax, NodeRes* res,
-                                                 Queues Q) {
+                                                 Queues Q, long long* stats) {
   __shared__ int sm[BLOCK / 32];
   __shared__ int s_cnt[kMaxClasses];
   __shared__ unsigned long long s_sum;
@@ -328,6 +337,10 @@ __global__ void __launch_bounds__(BLOCK) k_roots(const ProbDesc* probs, const in
   if (threadIdx.x < 32) {
     bool want = threadIdx.x == 0 && !preleaf(P, (int)s_n, 0);
     enqueue(Q, queue_of(P, out, Q.rf_small_cap), gt, want);
+    if (want) {
+      atomicAdd((unsigned long long*)&stats[0], (unsigned long long)out);
+      atomicAdd((unsigned long long*)&stats[1], s_n);
+    }
   }
 }
 
@@ -423,7 +436,7 @@ struct EmitArgs {
   int* next_cnt;
   NodeRes* next_res;
   Queues Q;
-  long long* stats;      // [0] entries of open nodes, [1] weighted rows
+  long long* stats;      // [0] entries of searched nodes, [1] their weighted rows
 };
 
 __global__ void __launch_bounds__(256) k_emit(EmitArgs a) {
@@ -509,8 +522,14 @@ __global__ void __launch_bounds__(256) k_emit(EmitArgs a) {
       s.leaf_cnt = a.leafpos[fe] - a.leafpos[fs];
       a.seg[f] = s;
     }
-    my_e = (unsigned long long)nd.ecnt;
-    my_w = (unsigned long long)nd.n;
+  }
+  if (wantL) {
+    my_e += (unsigned long long)a.next[cpL].ecnt;
+    my_w += (unsigned long long)a.next[cpL].n;
+  }
+  if (wantR) {
+    my_e += (unsigned long long)a.next[cpR].ecnt;
+    my_w += (unsigned long long)a.next[cpR].n;
   }
   my_e = warp_sum<unsigned long long>(my_e);
   my_w = warp_sum<unsigned long long>(my_w);
@@ -612,5 +631,7 @@ __global__ void k_to_pnodes(const ClassifyNode* nodes, long long n, const float*
     out[i] = p;
   }
 }
+
+#endif  // DML_SEARCH_CW
 
 }  // namespace dml

@@ -1,0 +1,8 @@
+// Split-search kernels instantiated for 1 packed class-count word(s).
+#define DML_SEARCH_CW 1
+#include "search_launch.cuh"
+
+namespace dml {
+template void launch_search_cw<1>(int, const LevelArgs&, int, cudaStream_t);
+template void launch_big_cw<1>(BigArgs, int, int, int, int, cudaStream_t);
+}  // namespace dml

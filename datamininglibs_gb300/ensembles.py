@@ -53,7 +53,8 @@ class ForestInfo(ctypes.Structure):
 
 class FitStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_int64), ("entries", ctypes.c_int64),
-                ("weighted_rows", ctypes.c_int64), ("levels", ctypes.c_int32),
+                ("weighted_rows", ctypes.c_int64), ("entry_tries", ctypes.c_int64),
+                ("levels", ctypes.c_int32),
                 ("launches", ctypes.c_int32), ("level_loop_ms", ctypes.c_double),
                 ("search_ms", ctypes.c_double)]
 

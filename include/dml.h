@@ -90,13 +90,14 @@ typedef struct {
 
 /* Fit statistics of the last dml_fit/dml_fit_batched on this thread. */
 typedef struct {
-  int64_t nodes;       /* internal + leaf nodes created, all forests */
-  int64_t entries;     /* sum over levels of the open nodes' row entries */
-  int64_t weighted_rows; /* sum over levels of the open nodes' weighted rows */
+  int64_t nodes;         /* internal + leaf nodes created, all forests */
+  int64_t entries;       /* sum over levels of the searched nodes' distinct row entries */
+  int64_t weighted_rows; /* the same with bootstrap multiplicities */
+  int64_t entry_tries;   /* sum over searched nodes of tries evaluated x entries */
   int32_t levels;
-  int32_t launches;    /* kernel launches of the fit */
-  double level_loop_ms; /* device time of the level loop (CUDA events) */
-  double search_ms;     /* device time in the split-search kernels */
+  int32_t launches;      /* kernel launches of the fit */
+  double level_loop_ms;  /* device time of the level loop (CUDA events) */
+  double search_ms;      /* device time in the split-search kernels */
 } dml_fit_stats;
 
 /* GpuDteAlgorithm<T>::Fit (lib_ensembles/source/gpudte_algorithm.cc:15-267),

@@ -487,7 +487,77 @@ bool is_leaf_rule(int64_t n, int depth, int min_node_size, int max_depth,
   return n <= min_node_size || depth >= max_depth || !valid_split;
 }
 
-void fit_tree(const Ctx& cx, int tree, TreeOut& out) {
+// One node of a level: search, leaf rule, partition.  Writes its output and,
+// for a split, its two children into ch[0..1] (has_children set).
+void fit_node(const Ctx& cx, int tree, int depth, size_t idx, OpenNode& nd,
+              std::vector<Entry>& E, std::vector<Entry>& E2, NodeOut& no,
+              OpenNode* ch, bool* has_children,
+              std::vector<std::pair<uint32_t, int32_t>>& sortbuf) {
+  const Problem& p = *cx.p;
+  const int C = p.n_classes;
+  const int64_t N = p.N;
+  *has_children = false;
+  no.is_leaf = 1;
+  no.attr = -1;
+  no.thr = -1.0f;
+  no.gain32 = NAN;
+  no.gain64 = NAN;
+  Cand best{false, -FLT_MAX, -1, 0.0f, 0.0};
+  if (nd.n > p.min_node_size && depth < p.max_depth) {
+    FF P{0.0f, 0.0f};
+    if (p.task == 0) {
+      P = (*cx.H)[nd.n];
+      for (int c = 0; c < C; ++c) P = ff_sub(P, (*cx.H)[nd.counts[c]]);
+    }
+    // try loop: gpuert.cu:144-149 / gpurf.cu:177-182
+    int K = p.K, F = p.F;
+    int n_mand = K < F ? K : F;
+    int n_opt = K < F ? std::min(F - K, 10) : 0;
+    int tr = 0;
+    for (; tr < n_mand; ++tr) {
+      W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)tree,
+                   (uint32_t)idx, (uint32_t)tr);
+      int f = (int)(w.v[0] % (uint32_t)F);
+      Cand c = eval_try(cx, E, nd, tree, depth, (int)idx, tr, f, P, sortbuf);
+      if (tr == 0 || better(c, best)) best = c;
+    }
+    if (!(best.valid && best.gain >= kSensible)) {
+      for (int j = 0; j < n_opt; ++j, ++tr) {
+        W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)tree,
+                     (uint32_t)idx, (uint32_t)tr);
+        int f = (int)(w.v[0] % (uint32_t)F);
+        Cand c = eval_try(cx, E, nd, tree, depth, (int)idx, tr, f, P, sortbuf);
+        if (better(c, best)) best = c;
+        if (c.valid && c.gain >= kSensible) break;
+      }
+    }
+  }
+  if (is_leaf_rule(nd.n, depth, p.min_node_size, p.max_depth, best.valid)) {
+    // leaf: payload = node class counts / node mean
+    if (p.task == 0)
+      no.counts = nd.counts;
+    else
+      no.value = (float)(((double)nd.sum * pow2d(-cx.S)) / (double)nd.n);
+    return;
+  }
+  // internal node: stable partition into children (left, right)
+  no.is_leaf = 0;
+  no.attr = best.f;
+  no.thr = best.thr;
+  no.gain32 = best.gain;
+  no.gain64 = best.gain64;
+  split_entries(E.data() + nd.ebeg, nd.ecnt, p.X + (int64_t)best.f * N, best.thr,
+                p.task, C, cx.lab.data(), cx.q.data(), E2.data() + nd.ebeg, &ch[0],
+                &ch[1]);
+  ch[0].ebeg += nd.ebeg;
+  ch[1].ebeg += nd.ebeg;
+  *has_children = true;
+}
+
+// Level-wise build of one tree.  With par_nodes the nodes of a level are
+// spread over OpenMP threads (each node owns its entry range and its output
+// slots, so the result does not depend on the thread count).
+void fit_tree(const Ctx& cx, int tree, TreeOut& out, bool par_nodes, int threads) {
   const Problem& p = *cx.p;
   const int C = p.n_classes;
   const int64_t N = p.N;
@@ -520,74 +590,34 @@ void fit_tree(const Ctx& cx, int tree, TreeOut& out) {
     else
       cur[0].sum += cx.q[e.row] * e.w;
   }
-  std::vector<std::pair<uint32_t, int32_t>> sortbuf;
   for (int depth = 0; !cur.empty(); ++depth) {
     out.levels.emplace_back();
     std::vector<NodeOut>& lv = out.levels.back();
-    lv.resize(cur.size());
-    nxt.clear();
-    for (size_t idx = 0; idx < cur.size(); ++idx) {
-      OpenNode& nd = cur[idx];
-      NodeOut& no = lv[idx];
-      no.is_leaf = 1;
-      no.attr = -1;
-      no.thr = -1.0f;
-      no.gain32 = NAN;
-      no.gain64 = NAN;
-      Cand best{false, -FLT_MAX, -1, 0.0f, 0.0};
-      if (nd.n > p.min_node_size && depth < p.max_depth) {
-        FF P{0.0f, 0.0f};
-        if (p.task == 0) {
-          P = (*cx.H)[nd.n];
-          for (int c = 0; c < C; ++c) P = ff_sub(P, (*cx.H)[nd.counts[c]]);
-        }
-        // try loop: gpuert.cu:144-149 / gpurf.cu:177-182
-        int K = p.K, F = p.F;
-        int n_mand = K < F ? K : F;
-        int n_opt = K < F ? std::min(F - K, 10) : 0;
-        int tr = 0;
-        for (; tr < n_mand; ++tr) {
-          W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)tree,
-                       (uint32_t)idx, (uint32_t)tr);
-          int f = (int)(w.v[0] % (uint32_t)F);
-          Cand c = eval_try(cx, E, nd, tree, depth, (int)idx, tr, f, P, sortbuf);
-          if (tr == 0 || better(c, best)) best = c;
-        }
-        if (!(best.valid && best.gain >= kSensible)) {
-          for (int j = 0; j < n_opt; ++j, ++tr) {
-            W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)tree,
-                         (uint32_t)idx, (uint32_t)tr);
-            int f = (int)(w.v[0] % (uint32_t)F);
-            Cand c = eval_try(cx, E, nd, tree, depth, (int)idx, tr, f, P,
-                              sortbuf);
-            if (better(c, best)) best = c;
-            if (c.valid && c.gain >= kSensible) break;
-          }
-        }
+    const size_t n = cur.size();
+    lv.resize(n);
+    std::vector<OpenNode> kids(2 * n);
+    std::vector<char> has(n, 0);
+#ifdef _OPENMP
+#pragma omp parallel num_threads(par_nodes ? threads : 1)
+#endif
+    {
+      std::vector<std::pair<uint32_t, int32_t>> sortbuf;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+      for (long long idx = 0; idx < (long long)n; ++idx) {
+        bool h = false;
+        fit_node(cx, tree, depth, (size_t)idx, cur[idx], E, E2, lv[idx], &kids[2 * idx],
+                 &h, sortbuf);
+        has[idx] = h;
       }
-      if (is_leaf_rule(nd.n, depth, p.min_node_size, p.max_depth, best.valid)) {
-        // leaf: payload = node class counts / node mean
-        if (p.task == 0)
-          no.counts = nd.counts;
-        else
-          no.value = (float)(((double)nd.sum * pow2d(-cx.S)) / (double)nd.n);
-        continue;
-      }
-      // internal node: stable partition into children (left, right)
-      no.is_leaf = 0;
-      no.attr = best.f;
-      no.thr = best.thr;
-      no.gain32 = best.gain;
-      no.gain64 = best.gain64;
-      OpenNode l, r;
-      split_entries(E.data() + nd.ebeg, nd.ecnt, p.X + (int64_t)best.f * N,
-                    best.thr, p.task, C, cx.lab.data(), cx.q.data(),
-                    E2.data() + nd.ebeg, &l, &r);
-      l.ebeg += nd.ebeg;
-      r.ebeg += nd.ebeg;
-      nxt.push_back(std::move(l));
-      nxt.push_back(std::move(r));
     }
+    nxt.clear();
+    for (size_t idx = 0; idx < n; ++idx)
+      if (has[idx]) {
+        nxt.push_back(std::move(kids[2 * idx]));
+        nxt.push_back(std::move(kids[2 * idx + 1]));
+      }
     // entries of split nodes were rewritten into E2; copy them back in place
     for (const OpenNode& ch : nxt)
       std::copy(E2.begin() + ch.ebeg, E2.begin() + ch.ebeg + ch.ecnt,
@@ -726,11 +756,18 @@ void* oracle_fit(const oracle_desc* d) {
   }
   cx.H = &H;
   std::vector<TreeOut> trees((size_t)p.n_trees);
+  int th = 1;
 #ifdef _OPENMP
-  int th = d->threads > 0 ? d->threads : omp_get_max_threads();
+  th = d->threads > 0 ? d->threads : omp_get_max_threads();
+#endif
+  if (p.n_trees >= th) {
+#ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 1) num_threads(th)
 #endif
-  for (int t = 0; t < p.n_trees; ++t) fit_tree(cx, t, trees[t]);
+    for (int t = 0; t < p.n_trees; ++t) fit_tree(cx, t, trees[t], false, 1);
+  } else {
+    for (int t = 0; t < p.n_trees; ++t) fit_tree(cx, t, trees[t], true, th);
+  }
 
   // level-major, tree-major assembly (gpudte_algorithm.cc:46-92 with a
   // deterministic order): roots 0..T-1, then level 1 of every tree, ...

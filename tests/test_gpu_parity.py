@@ -151,7 +151,23 @@ def test_missing_values_and_constant_features(dml, algo):
     assert np.array_equal(f.predict(Xq), oracle.predict(m, Xq))
 
 
-@pytest.mark.parametrize("n_rows", [1, 2, 3, 33, 4097])
+def test_big_nodes_with_signed_zeros_and_missing(dml):
+    """Nodes above the shared-memory sort size: thresholds next to -0/+0 and the
+    missing-value marker, classification and regression."""
+    X, y = synth.rf_multiclass(12000, 6, n_classes=3, n_int=2, seed=17)
+    X[1, ::3] = 0.0
+    X[1, 1::3] = -0.0
+    X[2, ::4] = -FLT_MAX
+    X[3] = np.where(X[3] > 0, -0.0, X[3])
+    for task in (0, 1):
+        yy = y if task == 0 else (y * 0.5 - 0.3).astype(np.float32)
+        kw = dict(algo=0, task=task, n_trees=3, K=4, max_depth=7, min_node_size=5,
+                  n_classes=3, seed=5)
+        m, f, nodes, probs = _fit_both(dml, X, yy, **kw)
+        _assert_same_model(m, nodes, probs, task)
+
+
+@pytest.mark.parametrize("n_rows", [1, 2, 3, 33, 65, 129, 257, 513, 4097])
 def test_tiny_and_boundary_sizes(dml, n_rows):
     X, y = synth.rf_multiclass(n_rows, 5, n_classes=2, n_int=1, seed=n_rows)
     for algo in (0, 1):
