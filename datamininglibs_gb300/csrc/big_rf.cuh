@@ -217,6 +217,9 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
                              long long* out_sl, unsigned long long (&outL)[CW]) {
   const int C = P.C;
   const int ml = max(1, P.min_leaf);
+  int Nt[2 * CW];
+#pragma unroll
+  for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
   float bg = -FLT_MAX;
   int bp = -1;
   long long bnl = 0, bsl = 0;
@@ -307,9 +310,13 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
         if (run_n >= ml && nr >= ml) {
           float g;
           if (P.task == 0)
-            g = entropy_gain(
-                H, prior, C, run_n, nr, [&](int c) { return packed_get<CW>(runL, c); },
-                [&](int c) { return (long long)ncnt[c]; });
+            g = entropy_gain_u<2 * CW>(
+                H, prior, C, run_n, nr,
+                [&](int c) {
+                  return (long long)((c & 1) ? (runL[c >> 1] >> 32)
+                                             : (runL[c >> 1] & 0xFFFFFFFFull));
+                },
+                [&](int c) { return (long long)Nt[c]; });
           else
             g = variance_gain(run_n, run_s, nr, nd.sum - run_s, P.S);
           if (bp < 0 || g > bg) {
@@ -343,7 +350,7 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
 }
 
 template <int CW>
-__global__ void __launch_bounds__(kBigBlock) k_rf_big_items(BigArgs b) {
+__global__ void __launch_bounds__(kBigBlock, 2) k_rf_big_items(BigArgs b) {
   __shared__ BigSmem S;
   __shared__ float s_g[kBigBlock];
   __shared__ int s_p[kBigBlock];
@@ -539,7 +546,7 @@ __global__ void __launch_bounds__(kBigBlock) k_rf_big_decide(BigArgs b) {
 // RF node of 257 .. SMEM_CAP entries in one CTA: keys and values sorted in
 // shared memory, then the same 8-per-thread boundary scan as the large path.
 template <int CW, int SMEM_CAP>
-__global__ void __launch_bounds__(kBigBlock) k_rf_smem(LevelArgs a) {
+__global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
   __shared__ SortSmem<kBigBlock> SS;
   __shared__ unsigned red[2 * kBigWarps];
   __shared__ unsigned long long scan64[kBigWarps];

@@ -165,6 +165,26 @@ __device__ __forceinline__ float entropy_gain(const float2* H, ff P, int C, long
   return __fdiv_rn(D.hi, den);
 }
 
+// The same with the class loop unrolled to a compile-time bound CMAX >= C,
+// so that per-class counts held in registers are read without index
+// arithmetic.  Identical operation order.
+template <int CMAX, class LeftFn, class TotFn>
+__device__ __forceinline__ float entropy_gain_u(const float2* H, ff P, int C, long long nL,
+                                                long long nR, LeftFn L, TotFn Ntot) {
+  ff Q{0.0f, 0.0f};
+  Q = ff_add(Q, ld_ff(H, nL));
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c)
+    if (c < C) Q = ff_sub(Q, ld_ff(H, L(c)));
+  Q = ff_add(Q, ld_ff(H, nR));
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c)
+    if (c < C) Q = ff_sub(Q, ld_ff(H, Ntot(c) - L(c)));
+  ff D = ff_sub(P, Q);
+  float den = __fmul_rn(__ll2float_rn(nL + nR), kLn2f);
+  return __fdiv_rn(D.hi, den);
+}
+
 __device__ __forceinline__ float variance_gain(long long nL, long long SL, long long nR,
                                                long long SR, int S) {
   ff mL = ff_div_f(ff_from_i64(SL), __ll2float_rn(nL));

@@ -10,7 +10,7 @@ namespace dml {
 // the 32 (key, lane) pairs with a register bitonic network; prefix class
 // counts come from warp scans.  Same candidate rules as the CTA kernels.
 template <int CW>
-__global__ void __launch_bounds__(256) k_warp_nodes(LevelArgs a) {
+__global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -30,6 +30,9 @@ __global__ void __launch_bounds__(256) k_warp_nodes(LevelArgs a) {
     const int k = (valid && P.task == 0) ? __ldg(P.lab + row) : -1;
     const long long qv = (valid && P.task == 1) ? __ldg(P.q + row) : 0;
     ff prior{0.0f, 0.0f};
+    int Nt[2 * CW];
+#pragma unroll
+    for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
     if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     Cand best;
     best.valid = 0;
@@ -113,16 +116,9 @@ __global__ void __launch_bounds__(256) k_warp_nodes(LevelArgs a) {
           for (int c = 0; c < 2 * CW; ++c)
             L[c] = c < C ? warp_excl_scan<int>(ke == c ? we : 0) : 0;
           if (bnd)
-            g = entropy_gain(
-                a.H, prior, C, nl, nr,
-                [&](int c) {
-                  int x = L[0];
-#pragma unroll
-                  for (int j = 1; j < 2 * CW; ++j)
-                    if (c == j) x = L[j];
-                  return (long long)x;
-                },
-                [&](int c) { return (long long)ncnt[c]; });
+            g = entropy_gain_u<2 * CW>(
+                a.H, prior, C, nl, nr, [&](int c) { return (long long)L[c]; },
+                [&](int c) { return (long long)Nt[c]; });
         } else {
           sl = warp_excl_scan<long long>(qe * (long long)we);
           if (bnd) g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);

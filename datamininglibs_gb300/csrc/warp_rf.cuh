@@ -68,7 +68,7 @@ constexpr int warp_rf_wpb() {
 }
 
 template <int E, int CW>
-__global__ void __launch_bounds__(32 * warp_rf_wpb<E>()) k_warp_rf(LevelArgs a) {
+__global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs a) {
   constexpr int M = 32 * E;
   constexpr int WPB = warp_rf_wpb<E>();
   __shared__ int s_row[WPB][M];
@@ -106,6 +106,9 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>()) k_warp_rf(LevelArgs a) 
     }
     __syncwarp();
     ff prior{0.0f, 0.0f};
+    int Nt[2 * CW];
+#pragma unroll
+    for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
     if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     Cand best;
     best.valid = 0;
@@ -173,9 +176,12 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>()) k_warp_rf(LevelArgs a) 
         if (bnd) {
           float g;
           if (P.task == 0)
-            g = entropy_gain(
-                a.H, prior, C, nl, nr, [&](int c) { return packed_get<CW>(L, c); },
-                [&](int c) { return (long long)ncnt[c]; });
+            g = entropy_gain_u<2 * CW>(
+                a.H, prior, C, nl, nr,
+                [&](int c) {
+                  return (long long)((c & 1) ? (L[c >> 1] >> 32) : (L[c >> 1] & 0xFFFFFFFFull));
+                },
+                [&](int c) { return (long long)Nt[c]; });
           else
             g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
           if (bp < 0 || g > bg) {
