@@ -784,6 +784,339 @@ static dml_status fit_entry(const dml_fit_desc* descs, int n, dml_forest** out, 
 
 }  // namespace dml
 
+// ---------------------------------------------------------------------------
+// Allocation-free fit.
+//
+// For callers that cannot allocate device memory while they fit: code that
+// runs while its stream is being captured into a CUDA graph, a host process
+// whose device memory is owned by its own allocator or partitioned by a
+// budget, or a latency-critical service that must not take the implicit device
+// synchronisation of cudaMalloc / cudaFree.  Every working buffer of the fit
+// comes from one file-scope device array of kNaArenaBytes (about 20 MiB) that
+// every GPU which loads this library holds until the process exits; the model
+// is written to device buffers the caller owns.  The problem must fit the
+// array: at most kNaMaxRows rows, n_trees * n_rows <= kNaMaxSlots, at most
+// kNaMaxClasses classes.  All calls share the array, so calls whose work
+// overlaps on the GPU (other streams, other host threads) race: serialise
+// them.  The first call on a device looks up the array's device address with
+// that device current; make that first call before any stream capture.
+namespace dml {
+namespace noalloc {
+constexpr long long kNaMaxRows = 4096;
+constexpr long long kNaMaxSlots = 65536;
+constexpr int kNaMaxClasses = 8;
+constexpr long long kNaMaxLevels = kNaMaxRows + 1;
+
+constexpr long long align256(long long x) { return (x + 255) / 256 * 256; }
+
+// byte offsets of the buffers inside the array
+constexpr long long oErr = 0;
+constexpr long long oMax = oErr + 256;
+constexpr long long oLab = oMax + 256;
+constexpr long long oQ = oLab + align256(4 * kNaMaxRows);
+constexpr long long oH = oQ + align256(8 * kNaMaxRows);
+constexpr long long oProb = oH + align256(8 * (kNaMaxRows + 1));
+constexpr long long oTreeProb = oProb + align256(sizeof(ProbDesc));
+constexpr long long oRowsA = oTreeProb + align256(4 * kNaMaxSlots);
+constexpr long long oRowsB = oRowsA + align256(4 * kNaMaxSlots);
+constexpr long long oWA = oRowsB + align256(4 * kNaMaxSlots);
+constexpr long long oWB = oWA + align256(4 * kNaMaxSlots);
+constexpr long long oBoot = oWB + align256(4 * kNaMaxSlots);
+constexpr long long oNodes0 = oBoot + align256(4 * kNaMaxSlots);
+constexpr long long oNodes1 = oNodes0 + align256(sizeof(LNode) * kNaMaxSlots);
+constexpr long long oCnt0 = oNodes1 + align256(sizeof(LNode) * kNaMaxSlots);
+constexpr long long oCnt1 = oCnt0 + align256(4 * kNaMaxClasses * kNaMaxSlots);
+constexpr long long oRes0 = oCnt1 + align256(4 * kNaMaxClasses * kNaMaxSlots);
+constexpr long long oRes1 = oRes0 + align256(sizeof(NodeRes) * kNaMaxSlots);
+constexpr long long oResCnt = oRes1 + align256(sizeof(NodeRes) * kNaMaxSlots);
+constexpr long long oChild = oResCnt + align256(4 * kNaMaxClasses * kNaMaxSlots);
+constexpr long long oLeaf = oChild + align256(4 * (kNaMaxSlots + 1));
+constexpr long long oParts = oLeaf + align256(4 * (kNaMaxSlots + 1));
+constexpr long long oQueues = oParts + align256(8 * (kNaMaxSlots / (kScanBlock * kScanItems) + 2));
+constexpr long long oQCount = oQueues + align256(4LL * kNumQ * kNaMaxSlots);
+constexpr long long oSummary = oQCount + 256;
+constexpr long long oStats = oSummary + 256;
+constexpr long long oBases = oStats + 256;
+constexpr long long oSeg = oBases + 256;
+constexpr long long kNaArenaBytes = oSeg + 256;
+}  // namespace noalloc
+}  // namespace dml
+
+static __device__ __align__(256) unsigned char g_noalloc_arena[dml::noalloc::kNaArenaBytes];
+
+namespace dml {
+namespace noalloc {
+constexpr int kMaxDevices = 64;
+static unsigned char* g_arena_dev[kMaxDevices];
+static std::mutex g_arena_mu;
+// host-side staging of the few values the driver reads back or uploads
+static float2 g_h_table[kNaMaxRows + 1];
+static int g_h_tree_prob[kNaMaxSlots];
+
+// The array's device address on the current device (looked up once per device).
+static unsigned char* arena_on_current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lk(g_arena_mu);
+  if (!g_arena_dev[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_arena);
+    if (e != cudaSuccess) {
+      set_error("cudaGetSymbolAddress of the allocation-free scratch failed: %s",
+                cudaGetErrorString(e));
+      return nullptr;
+    }
+    g_arena_dev[dev] = (unsigned char*)p;
+  }
+  return g_arena_dev[dev];
+}
+}  // namespace noalloc
+
+static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out,
+                                  long long node_cap, float* probs_out, long long prob_cap,
+                                  long long* n_nodes, long long* n_probs, cudaStream_t s) {
+  using namespace noalloc;
+  if (d.memory != DML_DEVICE) {
+    set_error("the allocation-free fit takes device pointers only");
+    return DML_ERR_INVALID_ARG;
+  }
+  if ((d.algo != DML_ALGO_RF && d.algo != DML_ALGO_ERT) ||
+      (d.task != DML_CLASSIFICATION && d.task != DML_REGRESSION) || d.n_trees <= 0 ||
+      d.n_rows <= 0 || d.n_features <= 0 || !d.samples || !d.targets || d.max_depth < 0 ||
+      d.min_node_size < 0 || d.n_features_try < 0 ||
+      (d.task == DML_CLASSIFICATION && d.n_classes < 1)) {
+    set_error("invalid fit parameters");
+    return DML_ERR_INVALID_ARG;
+  }
+  if (d.n_rows > kNaMaxRows || (long long)d.n_trees * d.n_rows > kNaMaxSlots ||
+      (d.task == DML_CLASSIFICATION && d.n_classes > kNaMaxClasses)) {
+    set_error("the allocation-free fit holds at most %lld rows, n_trees * n_rows <= %lld and "
+              "%d classes (got %lld rows, %d trees, %d classes)",
+              kNaMaxRows, kNaMaxSlots, kNaMaxClasses, (long long)d.n_rows, d.n_trees,
+              d.n_classes);
+    return DML_ERR_INVALID_ARG;
+  }
+  const int C = d.task == DML_CLASSIFICATION ? d.n_classes : 1;
+  const long long need_nodes = (long long)d.n_trees * (2 * d.n_rows - 1);
+  const long long need_probs = (long long)d.n_trees * d.n_rows * C;
+  if (!nodes_out || !probs_out || node_cap < need_nodes || prob_cap < need_probs) {
+    set_error("output buffers too small: need %lld nodes and %lld probabilities", need_nodes,
+              need_probs);
+    return DML_ERR_INVALID_ARG;
+  }
+  unsigned char* A = arena_on_current_device();
+  if (!A) {
+    if (last_error_str()[0] == 0) set_error("no scratch for this device");
+    return DML_ERR_CUDA;
+  }
+  try {
+    ProbDesc P;
+    std::memset(&P, 0, sizeof(P));
+    P.N = d.n_rows;
+    P.F = d.n_features;
+    P.C = C;
+    P.K = d.n_features_try > 0 ? d.n_features_try
+                               : (int)std::round(std::log((double)d.n_features)) + 1;
+    P.n_mand = std::min(P.K, P.F);
+    P.n_opt = P.K < P.F ? std::min(P.F - P.K, 10) : 0;
+    if (P.n_mand + P.n_opt > kMaxTries) {
+      set_error("at most %d tries per node", kMaxTries);
+      return DML_ERR_INVALID_ARG;
+    }
+    P.max_depth = d.max_depth;
+    P.min_node_size = d.min_node_size;
+    P.min_leaf = std::max(1, d.min_leaf);
+    P.algo = d.algo;
+    P.task = d.task;
+    P.seed = d.seed;
+    P.n_trees = d.n_trees;
+    P.tree0 = 0;
+    P.ent0 = 0;
+    P.X = d.samples;
+    P.lab = (int*)(A + oLab);
+    P.q = (long long*)(A + oQ);
+    const long long total_slots = (long long)d.n_trees * d.n_rows;
+    const int Cmax = C;
+    const int CW = Cmax <= 2 ? 1 : Cmax <= 4 ? 2 : 4;
+    int* d_err = (int*)(A + oErr);
+    unsigned* d_max = (unsigned*)(A + oMax);
+    DML_CK(cudaMemsetAsync(d_err, 0, 16, s));
+    DML_CK(cudaMemsetAsync(d_max, 0, 4, s));
+    const long long nx = P.N * P.F;
+    k_validate<<<(int)std::min<long long>(4096, (nx + 255) / 256), 256, 0, s>>>(
+        d.samples, nx, d.targets, P.N, P.task, P.C, d_err, d_max);
+    DML_CK(cudaGetLastError());
+    int h_err = 0;
+    unsigned h_max = 0;
+    DML_CK(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaMemcpyAsync(&h_max, d_max, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaStreamSynchronize(s));
+    if (h_err & 1) {
+      set_error("samples hold NaN or infinite values (the missing-value marker is -FLT_MAX)");
+      return DML_ERR_INVALID_ARG;
+    }
+    if (h_err & 2) {
+      set_error("classification targets must be integers in [0, n_classes)");
+      return DML_ERR_INVALID_ARG;
+    }
+    if (h_err & 4) {
+      set_error("regression targets hold NaN or infinite values");
+      return DML_ERR_INVALID_ARG;
+    }
+    float mx;
+    std::memcpy(&mx, &h_max, 4);
+    P.S = P.task == 1 ? quant_scale_from_max(mx, P.N) : 0;
+    k_prep_targets<<<(int)std::min<long long>(4096, (P.N + 255) / 256), 256, 0, s>>>(
+        d.targets, P.N, P.task, P.S, P.lab == nullptr ? nullptr : (int*)(A + oLab),
+        (long long*)(A + oQ));
+    DML_CK(cudaGetLastError());
+    const float2* H = nullptr;
+    if (P.task == 0) {
+      build_nlogn_table(P.N, g_h_table);
+      DML_CK(cudaMemcpyAsync(A + oH, g_h_table, sizeof(float2) * (P.N + 1),
+                             cudaMemcpyHostToDevice, s));
+      H = (const float2*)(A + oH);
+    }
+    ProbDesc* d_probs = (ProbDesc*)(A + oProb);
+    DML_CK(cudaMemcpyAsync(d_probs, &P, sizeof(ProbDesc), cudaMemcpyHostToDevice, s));
+    for (int t = 0; t < d.n_trees; ++t) g_h_tree_prob[t] = 0;
+    int* d_tree_prob = (int*)(A + oTreeProb);
+    DML_CK(cudaMemcpyAsync(d_tree_prob, g_h_tree_prob, sizeof(int) * d.n_trees,
+                           cudaMemcpyHostToDevice, s));
+    int* rowsA = (int*)(A + oRowsA);
+    int* rowsB = (int*)(A + oRowsB);
+    int* wA = d.algo == DML_ALGO_RF ? (int*)(A + oWA) : nullptr;
+    int* wB = d.algo == DML_ALGO_RF ? (int*)(A + oWB) : nullptr;
+    int* wcnt = (int*)(A + oBoot);
+    LNode* cur = (LNode*)(A + oNodes0);
+    LNode* nxt = (LNode*)(A + oNodes1);
+    int* cnt_cur = (int*)(A + oCnt0);
+    int* cnt_nxt = (int*)(A + oCnt1);
+    NodeRes* res_cur = (NodeRes*)(A + oRes0);
+    NodeRes* res_nxt = (NodeRes*)(A + oRes1);
+    int* res_cnt = (int*)(A + oResCnt);
+    int* childpos = (int*)(A + oChild);
+    int* leafpos = (int*)(A + oLeaf);
+    int2* parts = (int2*)(A + oParts);
+    int* d_qcount = (int*)(A + oQCount);
+    int* d_summary = (int*)(A + oSummary);
+    long long* d_stats = (long long*)(A + oStats);
+    long long* fbase[2] = {(long long*)(A + oBases), (long long*)(A + oBases) + 1};
+    long long* lbase[2] = {(long long*)(A + oBases) + 2, (long long*)(A + oBases) + 3};
+    Seg* seg = (Seg*)(A + oSeg);
+    DML_CK(cudaMemsetAsync(A + oBases, 0, 4 * sizeof(long long), s));
+    DML_CK(cudaMemsetAsync(d_stats, 0, 4 * sizeof(long long), s));
+    DML_CK(cudaMemsetAsync(d_qcount, 0, sizeof(int) * kNumQ, s));
+    Queues Q;
+    for (int i = 0; i < kNumQ; ++i) Q.list[i] = (int*)(A + oQueues) + (long long)i * kNaMaxSlots;
+    Q.count = d_qcount;
+    Q.rf_small_cap = kSmemCap;
+    if (d.algo == DML_ALGO_RF) {
+      DML_CK(cudaMemsetAsync(wcnt, 0, sizeof(int) * total_slots, s));
+      const int chunk = 1 << 16;
+      dim3 g((unsigned)((P.N + chunk - 1) / chunk), (unsigned)d.n_trees);
+      k_boot_count<<<g, 256, 0, s>>>(d_probs, d_tree_prob, wcnt, chunk);
+      DML_CK(cudaGetLastError());
+    }
+    k_roots<1024><<<d.n_trees, 1024, 0, s>>>(d_probs, d_tree_prob, wcnt, rowsA, wA, cur,
+                                             cnt_cur, Cmax, res_cur, Q, d_stats);
+    DML_CK(cudaGetLastError());
+    int qc[kNumQ];
+    DML_CK(cudaMemcpyAsync(qc, d_qcount, sizeof(int) * kNumQ, cudaMemcpyDeviceToHost, s));
+    DML_CK(cudaStreamSynchronize(s));
+    int n = d.n_trees;
+    long long log_base = 0, plog_base = 0;
+    int depth = 0;
+    while (n > 0) {
+      if (depth >= kNaMaxLevels) {
+        set_error("tree deeper than the allocation-free fit supports");
+        return DML_ERR_INTERNAL;
+      }
+      LevelArgs a;
+      std::memset(&a, 0, sizeof(a));
+      a.probs = d_probs;
+      a.nodes = cur;
+      a.cnt = cnt_cur;
+      a.Cmax = Cmax;
+      a.res = res_cur;
+      a.res_cnt = res_cnt;
+      a.rowsA = rowsA;
+      a.wA = wA;
+      a.rowsB = rowsB;
+      a.wB = wB;
+      a.scratch = nullptr;  // every node of <= kNaMaxRows entries sorts in shared memory
+      a.scratch_half = 0;
+      a.H = H;
+      a.stats = d_stats;
+      for (int q = 0; q < kNumQ; ++q) {
+        if (qc[q] <= 0) continue;
+        if (q == kQRfBig) {
+          set_error("internal: node too large for the allocation-free fit");
+          return DML_ERR_INTERNAL;
+        }
+        a.work = Q.list[q];
+        launch_search(CW, q, a, qc[q], s);
+      }
+      const int nparts = (n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
+      k_scan_part<<<nparts, kScanBlock, 0, s>>>(res_cur, n, parts);
+      k_scan_top<<<1, kScanBlock, 0, s>>>(parts, nparts, childpos, leafpos, n, d_summary);
+      k_scan_apply<<<nparts, kScanBlock, 0, s>>>(res_cur, n, parts, childpos, leafpos);
+      DML_CK(cudaGetLastError());
+      DML_CK(cudaMemsetAsync(d_qcount, 0, sizeof(int) * kNumQ, s));
+      DML_CK(cudaMemcpyAsync(fbase[(depth + 1) & 1], fbase[depth & 1], sizeof(long long),
+                             cudaMemcpyDeviceToDevice, s));
+      DML_CK(cudaMemcpyAsync(lbase[(depth + 1) & 1], lbase[depth & 1], sizeof(long long),
+                             cudaMemcpyDeviceToDevice, s));
+      EmitArgs e;
+      e.probs = d_probs;
+      e.cur = cur;
+      e.cnt = cnt_cur;
+      e.res = res_cur;
+      e.res_cnt = res_cnt;
+      e.childpos = childpos;
+      e.leafpos = leafpos;
+      e.n = n;
+      e.Cmax = Cmax;
+      e.log_base = log_base;
+      e.plog_base = plog_base;
+      e.node_log = nodes_out;   // one forest: log order is the model order
+      e.prob_log = probs_out;   // Cmax == C: leaf payloads packed
+      e.fbase_cur = fbase[depth & 1];
+      e.lbase_cur = lbase[depth & 1];
+      e.fbase_next = fbase[(depth + 1) & 1];
+      e.lbase_next = lbase[(depth + 1) & 1];
+      e.seg = seg;
+      e.next = nxt;
+      e.next_cnt = cnt_nxt;
+      e.next_res = res_nxt;
+      e.Q = Q;
+      e.stats = d_stats;
+      k_emit<<<(n + 255) / 256, 256, 0, s>>>(e);
+      DML_CK(cudaGetLastError());
+      int summary[2];
+      DML_CK(cudaMemcpyAsync(summary, d_summary, sizeof(summary), cudaMemcpyDeviceToHost, s));
+      DML_CK(cudaMemcpyAsync(qc, d_qcount, sizeof(int) * kNumQ, cudaMemcpyDeviceToHost, s));
+      DML_CK(cudaStreamSynchronize(s));
+      log_base += n;
+      plog_base += summary[1];
+      n = summary[0];
+      std::swap(cur, nxt);
+      std::swap(cnt_cur, cnt_nxt);
+      std::swap(res_cur, res_nxt);
+      std::swap(rowsA, rowsB);
+      std::swap(wA, wB);
+      ++depth;
+    }
+    *n_nodes = log_base;
+    *n_probs = plog_base * C;
+    return DML_OK;
+  } catch (CudaError& e) {
+    return DML_ERR_CUDA;
+  }
+}
+
+}  // namespace dml
+
 extern "C" {
 
 dml_status dml_fit(const dml_fit_desc* desc, dml_forest** out, void* stream) {
@@ -796,6 +1129,22 @@ dml_status dml_fit_batched(int32_t n, const dml_fit_desc* descs, dml_forest** ou
 
 dml_status dml_fit_plain(const dml_fit_desc* desc, dml_forest** out, void* stream) {
   return dml::fit_entry(desc, 1, out, stream, true);
+}
+
+dml_status dml_fit_noalloc(const dml_fit_desc* desc, void* node_array, int64_t node_capacity,
+                           float* probs, int64_t prob_capacity, int64_t* n_nodes,
+                           int64_t* n_probs, void* stream) {
+  dml::clear_error();
+  if (!desc || !n_nodes || !n_probs) {
+    dml::set_error("null argument");
+    return DML_ERR_INVALID_ARG;
+  }
+  long long nn = 0, np = 0;
+  dml_status st = dml::run_fit_noalloc(*desc, (dml::ClassifyNode*)node_array, node_capacity,
+                                       probs, prob_capacity, &nn, &np, (cudaStream_t)stream);
+  *n_nodes = nn;
+  *n_probs = np;
+  return st;
 }
 
 dml_status dml_last_fit_stats(dml_fit_stats* stats) {

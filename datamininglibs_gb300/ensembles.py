@@ -83,6 +83,10 @@ _SIGS = {
     "dml_fit_plain": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_void_p]),
     "dml_last_fit_stats": (ctypes.c_int, [ctypes.POINTER(FitStats)]),
+    "dml_fit_noalloc": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.c_void_p, ctypes.c_int64,
+                                       ctypes.c_void_p, ctypes.c_int64,
+                                       ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
     "dml_predict": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                    ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
     "dml_forest_info_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForestInfo)]),
@@ -237,6 +241,18 @@ def fit_plain(X, y, *, algo, task=CLASSIFICATION, n_trees=100, K=0, max_depth=10
     h = ctypes.c_void_p()
     _check(lib().dml_fit_plain(ctypes.byref(d), ctypes.byref(h), _stream(stream)))
     return Forest(h.value)
+
+
+def fit_noalloc(X, y, nodes_out, probs_out, *, algo, task=CLASSIFICATION, n_trees=100, K=0,
+                max_depth=1000, min_node_size=5, min_leaf=1, n_classes=2, seed=0, stream=None):
+    """dml_fit_noalloc: X, y and the two output buffers are CUDA tensors; the
+    fit allocates no device memory.  Returns (n_nodes, n_probs) written."""
+    d = _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed)
+    nn, npb = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().dml_fit_noalloc(ctypes.byref(d), nodes_out.data_ptr(), nodes_out.shape[0],
+                                 probs_out.data_ptr(), probs_out.numel(), ctypes.byref(nn),
+                                 ctypes.byref(npb), _stream(stream)))
+    return nn.value, npb.value
 
 
 def fit_batched(problems, stream=None):

@@ -117,6 +117,26 @@ DML_API dml_status dml_fit_batched(int32_t n, const dml_fit_desc* descs, dml_for
  * batched level path is measured against. */
 DML_API dml_status dml_fit_plain(const dml_fit_desc* desc, dml_forest** out, void* stream);
 
+/* No counterpart in the reference.  dml_fit for callers that cannot allocate
+ * device memory while they fit (a stream being captured into a CUDA graph, a
+ * process whose device memory belongs to its own allocator or budget, a
+ * latency-critical service that must avoid the device synchronisation of
+ * cudaMalloc/cudaFree).  Same trees as dml_fit.  It allocates nothing: its
+ * working buffers live in one static device array of about 20 MiB that every
+ * GPU loading this library holds until the process exits, so the problem must
+ * fit it: at most 4096 rows, n_trees * n_rows <= 65536, at most 8 classes;
+ * larger problems are rejected with DML_ERR_INVALID_ARG.  samples and targets
+ * must be device pointers (desc->memory == DML_DEVICE).  The model is written
+ * to caller-owned device buffers: node_array (Classify layout, 20 bytes per
+ * node, room for n_trees * (2 * n_rows - 1) nodes) and probs (room for
+ * n_trees * n_rows * n_classes floats); *n_nodes / *n_probs receive the sizes
+ * used.  Calls share the static array: calls whose work overlaps on the GPU
+ * race, so serialise them.  The first call on a device looks up the array's
+ * address with that device current and should come before any stream capture. */
+DML_API dml_status dml_fit_noalloc(const dml_fit_desc* desc, void* node_array,
+                                   int64_t node_capacity, float* probs, int64_t prob_capacity,
+                                   int64_t* n_nodes, int64_t* n_probs, void* stream);
+
 DML_API dml_status dml_last_fit_stats(dml_fit_stats* stats);
 
 /* GpuDteAlgorithm<T>::Predict (gpudte_algorithm.cc:270-331).  samples is
