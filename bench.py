@@ -166,6 +166,115 @@ def run_reference(args, w):
     print(json.dumps(line), flush=True)
 
 
+def batched_leg(dml, torch, stream):
+    """256 uneven ERT problems (rows log-uniform 200..50,000, features 8..256,
+    2..8 classes, 16 trees each, depth 16, min node size 5) fitted together,
+    one at a time, and with the plain chunked launch structure."""
+    from datamininglibs_gb300 import synth
+    probs = synth.uneven_problems(256, seed=0)
+    specs = [dict(X=torch.from_numpy(X).cuda(), y=torch.from_numpy(y).cuda(), algo=1,
+                  n_trees=16, K=0, max_depth=16, min_node_size=5, n_classes=c, seed=i)
+             for i, (X, y, c) in enumerate(probs)]
+    for _ in range(2):
+        for f in dml.fit_batched(specs, stream=stream):
+            f.free()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        fs = dml.fit_batched(specs, stream=stream)
+        nodes = sum(f.info().n_nodes for f in fs)
+        keep = fs[:32]
+        for f in fs[32:]:
+            f.free()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+
+    def one_by_one(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for sp in specs:
+            sp = dict(sp)
+            X, y = sp.pop("X"), sp.pop("y")
+            fn(X, y, stream=stream, **sp).free()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+    t_single = one_by_one(dml.fit)
+    t_plain = one_by_one(dml.fit_plain)
+    return {"workload": "256 uneven ERT forests x 16 trees", "nodes": nodes,
+            "nodes_per_s": nodes / dt, "ms": dt * 1e3,
+            "one_at_a_time_nodes_per_s": nodes / t_single,
+            "plain_path_nodes_per_s": nodes / t_plain,
+            "speedup_vs_plain": t_plain / dt}, keep, probs[:32]
+
+
+def serve_leg(dml, torch, stream, c2_forest, c4_forests, c4_probs):
+    """Resident forests (the ERT binary, RF multiclass and RF regression
+    workloads plus 32 of the uneven forests), Poisson arrivals at 100k req/s
+    offered, request rows log-uniform in [1, 65536], forest chosen uniformly."""
+    from datamininglibs_gb300 import synth
+    X1, y1 = synth.ert_binary()
+    f1 = dml.fit(X1, y1, algo=1, n_trees=64, K=7, max_depth=12, min_node_size=10, n_classes=2,
+                 seed=0)
+    X3, y3 = synth.rf_regression()
+    f3 = dml.fit(torch.from_numpy(X3).cuda(), torch.from_numpy(y3).cuda(), algo=0, task=1,
+                 n_trees=64, K=21, max_depth=24, min_node_size=5, min_leaf=5, seed=0,
+                 stream=stream)
+    del X3, y3
+    forests = [(f1, "ert_binary"), (c2_forest, "rf_multiclass"), (f3, "rf_regression")]
+    forests += [(f, "normal") for f in c4_forests]
+    rng = np.random.default_rng(5)
+    pools = {k: np.ascontiguousarray(synth.request_rows(rng, 65536, 256, k).reshape(-1))
+             for k in ("ert_binary", "rf_regression", "normal")}
+    pools["rf_multiclass"] = pools["normal"]
+    srv = dml.Server(hbm_budget_bytes=4 << 30, max_batch_rows=1 << 20, n_streams=4,
+                     max_wait_us=50)
+    fids = [srv.add_forest(f) for f, _ in forests]
+    infos = [f.info() for f, _ in forests]
+    ring = np.empty(1 << 26, np.float32)
+    M = 6000
+    rate = 100_000.0
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, M))
+    sizes = np.exp(rng.uniform(0.0, np.log(65536.0), M)).astype(np.int64)
+    which = rng.integers(0, len(forests), M)
+    reqs = []
+    for i in range(M):
+        fi = int(which[i])
+        F = infos[fi].n_features
+        n = int(sizes[i])
+        X = pools[forests[fi][1]][: F * n].reshape(F, n)
+        width = infos[fi].n_classes
+        off = (i * 997 * 64) % (ring.size - n * width)
+        reqs.append((fi, X, ring[off: off + n * width].reshape(n, width), n))
+    t0 = time.perf_counter()
+    ids = []
+    for i, (fi, X, out, n) in enumerate(reqs):
+        while time.perf_counter() - t0 < arrivals[i]:
+            pass
+        ids.append(srv.submit(fids[fi], X, out))
+    t_submit = time.perf_counter() - t0
+    lat = np.array([srv.wait(r) for r in ids])
+    st = srv.stats()
+    small = np.array([r[3] <= 4096 for r in reqs])
+    srv.close()
+    # the plain path: each request alone through dml_predict, one after another
+    torch.cuda.synchronize()
+    tp = time.perf_counter()
+    rows = 0
+    for fi, X, out, n in reqs[:1500]:
+        forests[fi][0].predict(X, out=out)
+        rows += n
+    plain_rows_per_s = rows / (time.perf_counter() - tp)
+    f1.free()
+    f3.free()
+    return {"requests": M, "offered_req_per_s": M / t_submit, "rows_per_s": st.rows_per_s,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "p50_ms_le4k": float(np.percentile(lat[small], 50)),
+            "p99_ms_le4k": float(np.percentile(lat[small], 99)),
+            "launches": st.launches, "plain_rows_per_s": plain_rows_per_s,
+            "speedup_vs_plain": st.rows_per_s / plain_rows_per_s}
+
+
 def run_ours(args, w):
     import torch
 
@@ -242,7 +351,6 @@ def run_ours(args, w):
     torch.cuda.synchronize()
     predict_rows_per_s = 3 * w["rows"] / (pe0.elapsed_time(pe1) / 1000.0)
     finfo = last_forest.info()
-    last_forest.free()
 
     # e2e: the C ABI with pinned host buffers, upload and model download timed
     Xh = torch.from_numpy(X).pin_memory()
@@ -262,6 +370,20 @@ def run_ours(args, w):
     e2e_s = time.perf_counter() - t0
     h2d = X.nbytes + y.nbytes
 
+    extras = {}
+    if world == 1 and not args.no_extras:
+        # the reference-structured plain path on the same workload
+        torch.cuda.synchronize()
+        tp = time.perf_counter()
+        fp = dml.fit_plain(Xd, yd, stream=stream, **kw)
+        torch.cuda.synchronize()
+        extras["plain_path"] = {"nodes_per_s": fp.info().n_nodes / (time.perf_counter() - tp)}
+        fp.free()
+        extras["batched_uneven"], c4f, c4p = batched_leg(dml, torch, stream)
+        extras["serve"] = serve_leg(dml, torch, stream, last_forest, c4f, c4p)
+        for f in c4f:
+            f.free()
+    last_forest.free()
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -299,6 +421,7 @@ def run_ours(args, w):
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    line.update(extras)
     if world == 1 and not args.no_cpu:
         th = os.cpu_count() or 1
         line["cpu_baseline"] = cpu_baseline(w, X, y, th, th)
@@ -315,6 +438,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="a reduced workload for quick checks")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the plain-path, batched-forest and serving legs")
     args = ap.parse_args()
     w = SMALL if args.small else WORKLOAD
     if args.impl == "reference":

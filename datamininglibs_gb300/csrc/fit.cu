@@ -677,6 +677,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       DML_CK(cudaMemcpyAsync(hseg.data(), segs.p, sizeof(Seg) * hseg.size(),
                              cudaMemcpyDeviceToHost, s));
     DML_CK(cudaStreamSynchronize(s));
+    std::vector<GatherSeg> gsegs;
     for (int i = 0; i < nprob; ++i) {
       dml_forest* f = new dml_forest();
       forests.push_back(f);
@@ -702,21 +703,30 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           const Seg& sg = hseg[(size_t)d * nprob + i];
           if (sg.node_cnt <= 0) continue;
           f->max_depth = d;
-          k_gather_nodes<<<(sg.node_cnt + 255) / 256, 256, 0, s>>>(node_log.p, sg.node_pos,
-                                                                   sg.node_cnt, f->nodes + no);
-          ++st.launches;
+          GatherSeg g;
+          g.node_pos = sg.node_pos;
+          g.node_cnt = sg.node_cnt;
+          g.node_dst = f->nodes + no;
+          g.leaf_rank = sg.leaf_rank;
+          g.leaf_cnt = sg.leaf_cnt;
+          g.C = hp[i].C;
+          g.prob_dst = f->probs + po;
+          gsegs.push_back(g);
           no += sg.node_cnt;
-          if (sg.leaf_cnt > 0) {
-            long long tot = sg.leaf_cnt * hp[i].C;
-            int g = (int)std::min<long long>(4096, (tot + 255) / 256);
-            k_gather_probs<<<g, 256, 0, s>>>(prob_log.p, sg.leaf_rank, sg.leaf_cnt, Cmax,
-                                             hp[i].C, f->probs + po);
-            ++st.launches;
-            po += tot;
-          }
+          po += sg.leaf_cnt * hp[i].C;
         }
-        DML_CK(cudaGetLastError());
       }
+    }
+    if (!gsegs.empty()) {
+      GatherSeg* d_gsegs = (GatherSeg*)alloc(sizeof(GatherSeg) * gsegs.size());
+      DML_CK(cudaMemcpyAsync(d_gsegs, gsegs.data(), sizeof(GatherSeg) * gsegs.size(),
+                             cudaMemcpyHostToDevice, s));
+      k_gather_segments<<<(unsigned)gsegs.size(), 256, 0, s>>>(d_gsegs, node_log.p, prob_log.p,
+                                                               Cmax);
+      DML_CK(cudaGetLastError());
+      ++st.launches;
+    }
+    for (dml_forest* f : forests) {
       dml_status ps = forest_build_pnodes(f, s);
       if (ps != DML_OK) throw CudaError{cudaErrorUnknown};
       ++st.launches;

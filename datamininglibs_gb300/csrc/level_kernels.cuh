@@ -575,6 +575,28 @@ __global__ void k_prep_targets(const float* y, long long N, int task, int S, int
   }
 }
 
+// One launch for every (level, forest) segment of a batch: nodes from the
+// node log into the forest's array, leaf payloads from the strided
+// probability log into the forest's packed array.
+struct GatherSeg {
+  long long node_pos, leaf_rank, leaf_cnt;
+  ClassifyNode* node_dst;
+  float* prob_dst;
+  int node_cnt, C;
+};
+
+__global__ void k_gather_segments(const GatherSeg* segs, const ClassifyNode* log,
+                                  const float* plog, int Cmax) {
+  const GatherSeg g = segs[blockIdx.x];
+  for (int i = threadIdx.x; i < g.node_cnt; i += blockDim.x) g.node_dst[i] = log[g.node_pos + i];
+  const long long tot = g.leaf_cnt * g.C;
+  for (long long i = threadIdx.x; i < tot; i += blockDim.x) {
+    const long long l = i / g.C;
+    const int c = (int)(i % g.C);
+    g.prob_dst[i] = plog[(g.leaf_rank + l) * Cmax + c];
+  }
+}
+
 // Probabilities from the strided log into a forest's packed array, and the
 // nodes of each (level, forest) segment into the forest's node array.
 __global__ void k_gather_nodes(const ClassifyNode* log, long long pos, int cnt, ClassifyNode* dst) {
