@@ -55,7 +55,25 @@ def build(verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_shim()
     return LIB
+
+
+SHIM_SRC = os.path.join(HERE, "shim", "src", "shim.cc")
+SHIM_LIB = os.path.join(HERE, "libdml_gb300_shim.so")
+
+
+def build_shim():
+    """The C++ drop-in (shim/include/datamininglibs.h) over the C ABI."""
+    tmp = SHIM_LIB + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall",
+           "-I" + os.path.join(HERE, "shim", "include"), SHIM_SRC, "-o", tmp,
+           "-L" + HERE, "-ldml_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("shim build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, SHIM_LIB)
+    return SHIM_LIB
 
 
 if __name__ == "__main__":

@@ -20,6 +20,7 @@ struct ProbDesc {
   int n_trees;
   int tree0;               // global index of tree 0 of this forest in the batch
   long long ent0;          // entry slot of tree 0; tree t owns [ent0 + t*N, +N)
+  int tree_key0;           // RNG tree key of tree 0 (trees sharded across calls)
 };
 
 // An open node of the current level.  Levels are stored forest-major,

@@ -244,7 +244,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       set_error("forest %d: n_classes must be in [1, %d]", i, kMaxClasses);
       throw InvalidArg{};
     }
-    if (d.max_depth < 0 || d.min_node_size < 0 || d.n_features_try < 0 ||
+    if (d.max_depth < 0 || d.min_node_size < 0 || d.n_features_try < 0 || d.tree_offset < 0 ||
         (d.memory != DML_HOST && d.memory != DML_DEVICE)) {
       set_error("forest %d: max_depth, min_node_size, n_features_try must be >= 0", i);
       throw InvalidArg{};
@@ -272,6 +272,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     P.task = d.task;
     P.seed = d.seed;
     P.n_trees = d.n_trees;
+    P.tree_key0 = d.tree_offset;
     P.tree0 = total_trees;
     P.ent0 = total_slots;
     total_trees += d.n_trees;
@@ -940,6 +941,7 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
     P.task = d.task;
     P.seed = d.seed;
     P.n_trees = d.n_trees;
+    P.tree_key0 = d.tree_offset;
     P.tree0 = 0;
     P.ent0 = 0;
     P.X = d.samples;

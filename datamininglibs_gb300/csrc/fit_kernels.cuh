@@ -80,7 +80,8 @@ __device__ __forceinline__ bool better(const Cand& a, const Cand& b) {
 }
 
 __device__ __forceinline__ int feature_of_try(const ProbDesc& P, const LNode& nd, int t) {
-  U4 w = keyed(P.seed, kTagFeature, (uint32_t)nd.depth, (uint32_t)nd.tree, (uint32_t)nd.idx,
+  U4 w = keyed(P.seed, kTagFeature, (uint32_t)nd.depth, (uint32_t)(nd.tree + P.tree_key0),
+               (uint32_t)nd.idx,
                (uint32_t)t);
   return (int)(w.x % (uint32_t)P.F);
 }
@@ -93,7 +94,8 @@ __device__ __forceinline__ float ert_threshold(const ProbDesc& P, const LNode& n
   float v[10];
 #pragma unroll
   for (int g = 0; g < 3; ++g) {
-    U4 w = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)nd.tree, (uint32_t)nd.idx,
+    U4 w = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)(nd.tree + P.tree_key0),
+                 (uint32_t)nd.idx,
                  (uint32_t)(t * 3 + g));
 #pragma unroll
     for (int s = 0; s < 4; ++s) {

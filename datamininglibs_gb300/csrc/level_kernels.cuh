@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
       if (P.algo == 1) {  // ERT
         float sv = 0.0f;
         if (lane < 10) {
-          U4 r = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)nd.tree,
+          U4 r = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)(nd.tree + P.tree_key0),
                        (uint32_t)nd.idx, (uint32_t)(t * 3 + lane / 4));
           uint32_t pos = pick(r, lane & 3) % (uint32_t)m;
           sv = __ldg(xf + __ldg(rows + pos));
@@ -257,7 +257,8 @@ __global__ void k_boot_count(const ProbDesc* probs, const int* tree_prob, int* w
   long long beg = (long long)blockIdx.x * chunk;
   long long end = min(P.N, beg + chunk);
   for (long long i = beg + threadIdx.x; i < end; i += blockDim.x) {
-    U4 r = keyed(P.seed, kTagBoot, 0, (uint32_t)t, (uint32_t)(i >> 2), (uint32_t)(i >> 34));
+    U4 r = keyed(P.seed, kTagBoot, 0, (uint32_t)(t + P.tree_key0), (uint32_t)(i >> 2),
+                 (uint32_t)(i >> 34));
     uint32_t row = pick(r, (int)(i & 3)) % (uint32_t)P.N;
     atomicAdd(&wcnt[slot0 + row], 1);
   }

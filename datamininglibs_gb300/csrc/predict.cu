@@ -217,6 +217,30 @@ dml_status dml_forest_import(int32_t task, int32_t n_trees, int32_t n_classes, i
   return DML_OK;
 }
 
+dml_status dml_device_count(int32_t* count) {
+  if (!count) return DML_ERR_INVALID_ARG;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *count = 0;
+    set_error("no CUDA device: %s", cudaGetErrorString(e));
+    return DML_ERR_CUDA;
+  }
+  *count = n;
+  return DML_OK;
+}
+
+dml_status dml_set_device(int32_t device) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cannot select device %d: %s", device, cudaGetErrorString(e));
+    return DML_ERR_CUDA;
+  }
+  return DML_OK;
+}
+
 void dml_forest_free(dml_forest* f) {
   if (!f) return;
   cudaFree(f->nodes);

@@ -40,7 +40,8 @@ class FitDesc(ctypes.Structure):
                 ("min_leaf", ctypes.c_int32), ("n_classes", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("n_rows", ctypes.c_int64),
                 ("n_features", ctypes.c_int32), ("memory", ctypes.c_int32),
-                ("samples", ctypes.c_void_p), ("targets", ctypes.c_void_p)]
+                ("samples", ctypes.c_void_p), ("targets", ctypes.c_void_p),
+                ("tree_offset", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class ForestInfo(ctypes.Structure):
@@ -96,6 +97,8 @@ _SIGS = {
                                          ctypes.c_void_p, ctypes.c_int64,
                                          ctypes.POINTER(ctypes.c_void_p)]),
     "dml_forest_free": (None, [ctypes.c_void_p]),
+    "dml_device_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
+    "dml_set_device": (ctypes.c_int, [ctypes.c_int32]),
     "dml_last_error": (ctypes.c_char_p, []),
     "dml_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig),
                                          ctypes.POINTER(ctypes.c_void_p)]),
@@ -216,20 +219,23 @@ class Forest:
         return Forest(h.value)
 
 
-def _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed):
+def _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed,
+          tree_offset=0):
     xp, mem = _ptr(X)
     yp, ymem = _ptr(y)
     if mem != ymem:
         raise ValueError("samples and targets must both be host or both device memory")
     F, N = X.shape
     return FitDesc(algo, task, n_trees, K, max_depth, min_node_size, min_leaf,
-                   n_classes if task == CLASSIFICATION else 1, seed, N, F, mem, xp, yp)
+                   n_classes if task == CLASSIFICATION else 1, seed, N, F, mem, xp, yp,
+                   tree_offset, 0)
 
 
 def fit(X, y, *, algo, task=CLASSIFICATION, n_trees=100, K=0, max_depth=1000,
-        min_node_size=5, min_leaf=1, n_classes=2, seed=0, stream=None):
+        min_node_size=5, min_leaf=1, n_classes=2, seed=0, tree_offset=0, stream=None):
     """Defaults are the reference's param pack (ensembles_interface.cc:28-58)."""
-    d = _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed)
+    d = _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed,
+              tree_offset)
     h = ctypes.c_void_p()
     _check(lib().dml_fit(ctypes.byref(d), ctypes.byref(h), _stream(stream)))
     return Forest(h.value)

@@ -72,6 +72,10 @@ typedef struct {
   int32_t memory; /* dml_memory of samples/targets */
   const float* samples;
   const float* targets;
+  /* RNG key of the first tree: a forest fitted as parts with tree_offset =
+   * the trees before each part equals the forest fitted at once. */
+  int32_t tree_offset;
+  int32_t reserved;
 } dml_fit_desc;
 
 typedef struct dml_forest dml_forest;
@@ -162,6 +166,13 @@ DML_API dml_status dml_forest_import(int32_t task, int32_t n_trees, int32_t n_cl
 DML_API void dml_forest_free(dml_forest* forest);
 
 DML_API const char* dml_last_error(void);
+
+/* GpuDevice::GetDeviceCount (lib_gpu/include/gpu_device.h:22) and the device
+ * choice of GpuInterface::CreateGpuDevice(dev_id) (lib_gpu/source/
+ * gpu_interface.cc:13-40) for the calling thread: the engine runs on the
+ * calling thread's current CUDA device. */
+DML_API dml_status dml_device_count(int32_t* count);
+DML_API dml_status dml_set_device(int32_t device);
 
 /* ------------------------------------------------------------------ serving
  * No reference counterpart (the reference has no serving path): a resident-

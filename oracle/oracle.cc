@@ -223,6 +223,7 @@ struct Problem {
   uint64_t seed;
   int64_t N;
   int F;
+  int tree_offset;  // RNG key of tree 0
   const float* X;  // feature-major [F*N]
   const float* y;  // [N]
 };
@@ -351,7 +352,7 @@ Cand eval_try(const Ctx& cx, const std::vector<Entry>& E, const OpenNode& nd,
     // ERT: threshold = mean of 10 node values drawn with replacement
     float acc = 0.0f;
     for (int s = 0; s < 10; ++s) {
-      W4 w = keyed(p.seed, kTagSample, (uint32_t)depth, (uint32_t)tree,
+      W4 w = keyed(p.seed, kTagSample, (uint32_t)depth, (uint32_t)(tree + p.tree_offset),
                    (uint32_t)idx, (uint32_t)(tr * 3 + s / 4));
       int64_t pos = (int64_t)(w.v[s % 4] % (uint32_t)m);
       acc = acc + xf[E[nd.ebeg + pos].row];
@@ -515,7 +516,7 @@ void fit_node(const Ctx& cx, int tree, int depth, size_t idx, OpenNode& nd,
     int n_opt = K < F ? std::min(F - K, 10) : 0;
     int tr = 0;
     for (; tr < n_mand; ++tr) {
-      W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)tree,
+      W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)(tree + p.tree_offset),
                    (uint32_t)idx, (uint32_t)tr);
       int f = (int)(w.v[0] % (uint32_t)F);
       Cand c = eval_try(cx, E, nd, tree, depth, (int)idx, tr, f, P, sortbuf);
@@ -523,7 +524,7 @@ void fit_node(const Ctx& cx, int tree, int depth, size_t idx, OpenNode& nd,
     }
     if (!(best.valid && best.gain >= kSensible)) {
       for (int j = 0; j < n_opt; ++j, ++tr) {
-        W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)tree,
+        W4 w = keyed(p.seed, kTagFeature, (uint32_t)depth, (uint32_t)(tree + p.tree_offset),
                      (uint32_t)idx, (uint32_t)tr);
         int f = (int)(w.v[0] % (uint32_t)F);
         Cand c = eval_try(cx, E, nd, tree, depth, (int)idx, tr, f, P, sortbuf);
@@ -566,7 +567,7 @@ void fit_tree(const Ctx& cx, int tree, TreeOut& out, bool par_nodes, int threads
   if (p.algo == 0) {
     std::vector<int32_t> w((size_t)N, 0);
     for (int64_t i = 0; i < N; ++i) {
-      W4 r = keyed(p.seed, kTagBoot, 0, (uint32_t)tree, (uint32_t)(i >> 2),
+      W4 r = keyed(p.seed, kTagBoot, 0, (uint32_t)(tree + p.tree_offset), (uint32_t)(i >> 2),
                    (uint32_t)(i >> 34));
       w[r.v[i & 3] % (uint32_t)N] += 1;
     }
@@ -651,6 +652,7 @@ typedef struct {
   int32_t n_features, threads;
   const float* samples;
   const float* targets;
+  int32_t tree_offset, reserved;
 } oracle_desc;
 
 // Philox4x32-10 known-answer access for tests.
@@ -739,6 +741,7 @@ void* oracle_fit(const oracle_desc* d) {
   p.N = d->n_rows;
   p.X = d->samples;
   p.y = d->targets;
+  p.tree_offset = d->tree_offset;
   Ctx cx;
   cx.p = &p;
   std::vector<FF> H;

@@ -22,6 +22,7 @@ class OracleDesc(ctypes.Structure):
         ("seed", ctypes.c_uint64), ("n_rows", ctypes.c_int64),
         ("n_features", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("samples", ctypes.c_void_p), ("targets", ctypes.c_void_p),
+        ("tree_offset", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 
@@ -89,14 +90,14 @@ class Model:
 
 
 def fit(X, y, *, algo, task=0, n_trees, K=0, max_depth=1000, min_node_size=5, min_leaf=1,
-        n_classes=2, seed=0, threads=0):
+        n_classes=2, seed=0, threads=0, tree_offset=0):
     """X: float32 feature-major [F, N]; y: float32 [N]."""
     X = np.ascontiguousarray(X, dtype=np.float32)
     y = np.ascontiguousarray(y, dtype=np.float32)
     F, N = X.shape
     d = OracleDesc(algo, task, n_trees, K, max_depth, min_node_size, min_leaf,
                    n_classes if task == 0 else 1, seed, N, F, threads,
-                   X.ctypes.data, y.ctypes.data)
+                   X.ctypes.data, y.ctypes.data, tree_offset, 0)
     L = lib()
     h = L.oracle_fit(ctypes.byref(d))
     nn, npb = ctypes.c_int64(), ctypes.c_int64()

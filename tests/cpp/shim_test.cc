@@ -1,0 +1,154 @@
+// Test driver of the C++ drop-in (datamininglibs_gb300/shim): written against
+// the reference's public API the way its tests are
+// (lib_ensembles/test/test_gpurf.h, test_gpuert.h).  Modes:
+//   parse <in.csv> <out.bin>   ParsingInterface::ParseFile<float>, dumped
+//   fit <data.bin> <out_dir>   RF fit/predict, split + aggregate, double frames
+#include <datamininglibs.h>
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+
+#define CHECK(x)                                                   \
+  do {                                                             \
+    if (!(x)) {                                                    \
+      std::cerr << "CHECK failed: " #x " line " << __LINE__ << "\n"; \
+      return 1;                                                    \
+    }                                                              \
+  } while (0)
+
+template <class T>
+static void dump(std::ofstream& f, const std::vector<T>& v) {
+  int64_t n = (int64_t)v.size();
+  f.write((const char*)&n, 8);
+  f.write((const char*)v.data(), sizeof(T) * v.size());
+}
+
+template <typename T>
+static std::vector<float> votes(const sp<lib_data::MlResultData<T>>& r) {
+  std::vector<float> out;
+  for (auto& row : r->GetPredictions())
+    for (auto v : row) out.push_back((float)v);
+  return out;
+}
+
+static std::vector<int32_t> raw_nodes(const sp<lib_models::MlModel>& m) {
+  using Node = lib_ensembles::GpuDteAlgorithmShared::gpuDTE_NodeHeader_Classify<float>;
+  auto& nodes = m->Get<std::vector<Node>>(ModelsLib::kNodeArray);
+  std::vector<int32_t> raw;
+  for (auto& n : nodes) {
+    int32_t sp;
+    std::memcpy(&sp, &n.split_point, 4);
+    raw.insert(raw.end(), {n.child_start, n.child_count, n.probability_start, n.attribute, sp});
+  }
+  return raw;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 4) return 2;
+  std::string mode = argv[1];
+  auto& parser = ParsingLib::GetInstance();
+  if (mode == "parse") {
+    try {
+      auto df = parser.ParseFile<float>(lib_parsing::ParsingInterface::kCsv, argv[2]);
+      std::ofstream f(argv[3], std::ios::binary);
+      int32_t hdr[3] = {df->GetNrSamples(), df->GetNrFeatures(), df->GetNrTargets()};
+      f.write((const char*)hdr, sizeof(hdr));
+      dump(f, df->GetSamples());
+      dump(f, df->GetTargets());
+    } catch (std::exception& e) {
+      std::cerr << "parse failed: " << e.what() << "\n";
+      return 3;
+    }
+    return 0;
+  }
+  if (mode != "fit") return 2;
+  // data.bin: int32 N, F, C; float X[F*N] (feature-major); float y[N]
+  std::ifstream in(argv[2], std::ios::binary);
+  int32_t N, F, C;
+  in.read((char*)&N, 4);
+  in.read((char*)&F, 4);
+  in.read((char*)&C, 4);
+  std::vector<float> X((size_t)N * F), y(N);
+  in.read((char*)X.data(), 4 * X.size());
+  in.read((char*)y.data(), 4 * y.size());
+  std::string dir = argv[3];
+
+  auto& ens = EnsemblesLib::GetInstance();
+  auto df = DataLib::GetInstance().CreateDataFrame<float>();
+  df->AddSampleData(X);
+  df->AddTargetData(y);
+  df->AddFeatureMap(std::vector<std::map<std::string, float>>(F));
+  std::map<std::string, float> tmap;
+  for (int c = 0; c < C; ++c) tmap[std::to_string(c)] = (float)c;
+  df->AddTargetMap(tmap);
+
+  auto rf = ens.CreateGpuRfAlgorithm<float>();
+  auto params = ens.CreateGpuRfParamPack();
+  params->Set(EnsemblesLib::kNrTrees, 12);
+  params->Set(EnsemblesLib::kAlgoType, AlgorithmsLib::kClassification);
+  params->Set(EnsemblesLib::kNrFeatures, 5);
+  params->Set(EnsemblesLib::kMaxDepth, 14);
+  params->Set(EnsemblesLib::kMinNodeSize, 5);
+  params->Set(EnsemblesLib::kMinLeaf, 2);
+  params->Set(EnsemblesLib::kSeed, 3);
+  auto model = rf->Fit(df, params);
+  CHECK(model->Get<int>(ModelsLib::kNrTrees) == 12);
+  auto res = rf->Predict(df, model, params);
+  float acc = res->GetAccuracy(df->GetTargets());
+  std::cout << "accuracy " << acc << "\n";
+  {
+    std::ofstream f(dir + "/model.bin", std::ios::binary);
+    dump(f, raw_nodes(model));
+    dump(f, model->Get<std::vector<float>>(ModelsLib::kProbArray));
+    dump(f, votes(res));
+  }
+  // the same forest fitted as three parts (tree offsets carried), aggregated
+  auto packs = rf->SplitParameterPack(params, 3);
+  std::vector<sp<lib_models::MlModel>> parts;
+  for (auto& p : packs) parts.push_back(rf->Fit(df, p));
+  auto agg = rf->AggregateModels(parts);
+  CHECK(agg->Get<int>(ModelsLib::kNrTrees) == 12);
+  CHECK(votes(rf->Predict(df, agg, params)) == votes(res));
+  // split a model, predict the parts, sum the votes
+  auto split = rf->SplitModel(model, 5);
+  std::vector<sp<lib_data::MlResultData<float>>> rs;
+  for (auto& m : split) rs.push_back(rf->Predict(df, m, params));
+  CHECK(votes(rf->AggregateResults(rs)) == votes(res));
+  // double frames give the same forest (values are narrowed to float)
+  auto dfd = DataLib::GetInstance().CreateDataFrame<double>();
+  dfd->AddSampleData(std::vector<double>(X.begin(), X.end()));
+  dfd->AddTargetData(std::vector<double>(y.begin(), y.end()));
+  dfd->AddFeatureMap(std::vector<std::map<std::string, double>>(F));
+  std::map<std::string, double> tmapd;
+  for (int c = 0; c < C; ++c) tmapd[std::to_string(c)] = (double)c;
+  dfd->AddTargetMap(tmapd);
+  auto rfd = ens.CreateGpuRfAlgorithm<double>();
+  auto md = rfd->Fit(dfd, params);
+  CHECK(votes(rfd->Predict(dfd, md, params)) == votes(res));
+  // ERT with the reference's default pack (K = round(ln F) + 1, 100 trees)
+  auto ert = ens.CreateGpuErtAlgorithm<float>();
+  auto ep = ens.CreateGpuErtParamPack();
+  auto me = ert->Fit(df, ep);
+  CHECK(me->Get<int>(ModelsLib::kNrTrees) == 100);
+  auto re = ert->Predict(df, me, ep);
+  {
+    std::ofstream f(dir + "/ert.bin", std::ios::binary);
+    dump(f, raw_nodes(me));
+    dump(f, me->Get<std::vector<float>>(ModelsLib::kProbArray));
+    dump(f, votes(re));
+  }
+  // errors surface as the reference's exception type
+  bool threw = false;
+  try {
+    auto bad = ens.CreateGpuRfParamPack();
+    bad->Set(EnsemblesLib::kNrTrees, 0);
+    rf->Fit(df, bad);
+  } catch (lib_core::template_exception& e) {
+    threw = std::string(e.what()).find("Fit") != std::string::npos;
+  }
+  CHECK(threw);
+  std::cout << "shim ok\n";
+  return 0;
+}

@@ -129,6 +129,7 @@ def main():
     csv = {}
     for key, text in fx.items():
         Xc, yc, nt = ref.parse_csv(text)
+        csv[key + "_text"] = np.array(text)
         csv[key + "_X"] = Xc
         csv[key + "_y"] = yc
         csv[key + "_ntargets"] = np.array(nt)

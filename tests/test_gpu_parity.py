@@ -234,3 +234,21 @@ def test_import_reference_layout_model(dml):
                    seed=1)
     f = dml.Forest.from_model(m.nodes, m.probs, task=0, n_trees=9, n_classes=2, n_features=10)
     assert np.array_equal(f.predict(X), oracle.predict(m, X))
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+def test_tree_offset_parts_equal_the_whole_forest(dml, algo):
+    """A forest fitted as parts (tree keys offset by the part's first tree, as
+    SplitParameterPack hands them out) votes exactly as the forest fitted in one
+    call, and each part equals the oracle's fit with the same offset."""
+    X, y = synth.rf_multiclass(2500, 18, n_classes=4, n_int=3, seed=31)
+    kw = dict(algo=algo, K=5, max_depth=12, min_node_size=5, n_classes=4, seed=17)
+    whole = dml.fit(X, y, n_trees=10, **kw).predict(X)
+    acc = np.zeros_like(whole)
+    for t0, k in ((0, 3), (3, 3), (6, 4)):
+        m = oracle.fit(X, y, n_trees=k, tree_offset=t0, **kw)
+        f = dml.fit(X, y, n_trees=k, tree_offset=t0, **kw)
+        nodes, probs = f.export()
+        _assert_same_model(m, nodes, probs, f"part at {t0}")
+        acc += f.predict(X)
+    assert np.array_equal(acc, whole)
