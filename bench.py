@@ -411,7 +411,7 @@ def run_ours(args, w):
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": (tpu * entry_tries / args.steps / max(1, launches))
                      if tpu else None,
-                     "kernel": "split search (k_rf_cta, k_warp_nodes)",
+                     "kernel": "split search (k_group_nodes, k_warp_rf, k_rf_smem, k_rf_big_items, k_ert_cta)",
                      "algorithmic_bytes_per_fit": alg_bytes / args.steps,
                      "peak_kind": peak_kind,
                      "search_ms_per_fit": search_ms / args.steps,

@@ -504,7 +504,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       int qc[kNumQ];
       std::memcpy(qc, h_sum->qcount, sizeof(qc));
       DML_CK(cudaEventRecord(es0, s));
-      float qms[kNumQ] = {0, 0, 0, 0, 0, 0, 0, 0};
+      float qms[kNumQ] = {};
       for (int q = 0; q < kNumQ; ++q) {
         if (qc[q] <= 0) continue;
         if (q == kQRfBig) {
@@ -631,11 +631,12 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       search_ms_total += sm;
       if (trace)
         fprintf(stderr,
-                "[dml] level %2d nodes %9d | w32 %8d %7.2f | ert %6d %7.2f | w64 %7d %7.2f | w128 %7d "
-                "%7.2f | w256 %7d %7.2f | w512 %7d %7.2f | cta %7d %7.2f | big %5d %7.2f | search "
-                "%8.2f ms\n",
-                depth, n, qc[0], qms[0], qc[1], qms[1], qc[4], qms[4], qc[5], qms[5], qc[6],
-                qms[6], qc[7], qms[7], qc[2], qms[2], qc[3], qms[3], sm);
+                "[dml] level %2d nodes %9d | g8 %8d %7.2f | g16 %8d %7.2f | w32 %8d %7.2f | ert %6d "
+                "%7.2f | w64 %7d %7.2f | w128 %7d %7.2f | w256 %7d %7.2f | cta %7d %7.2f | big %5d "
+                "%7.2f | search %8.2f ms\n",
+                depth, n, qc[kQG8], qms[kQG8], qc[kQG16], qms[kQG16], qc[kQWarp], qms[kQWarp],
+                qc[kQErt], qms[kQErt], qc[kQRfW2], qms[kQRfW2], qc[kQRfW4], qms[kQRfW4], qc[kQRfW8],
+                qms[kQRfW8], qc[kQRfSmall], qms[kQRfSmall], qc[kQRfBig], qms[kQRfBig], sm);
       log_base += n;
       plog_base += h_sum->leaves;
       n = h_sum->children;

@@ -6,27 +6,57 @@
 namespace dml {
 
 // ============================================================== tiny nodes
-// One warp per node with at most 32 entries: entries live in lanes.  RF sorts
-// the 32 (key, lane) pairs with a register bitonic network; prefix class
-// counts come from warp scans.  Same candidate rules as the CTA kernels.
-template <int CW>
-__global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
+// Groups of G lanes (G = 8, 16 or 32) per node with at most G entries, 32/G
+// nodes per warp: entries live in lanes.  RF sorts the (key, lane) pairs with a
+// register bitonic network; prefix class counts come from group scans.  Same
+// candidate rules as the CTA kernels.  Every shuffle and ballot names only the
+// group's lanes, so groups of one warp may hold nodes of different forests
+// (RF and ERT, classification and regression) and run different try counts.
+template <int G, class T>
+__device__ __forceinline__ T grp_excl_scan(T v, int gl, unsigned gm) {
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1) {
+    T y = __shfl_up_sync(gm, x, o, G);
+    if (gl >= o) x += y;
+  }
+  return x - v;
+}
+
+template <int G, class T>
+__device__ __forceinline__ T grp_sum(T v, unsigned gm) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gm, v, o, G);
+  return v;
+}
+
+template <int CW, int G>
+__global__ void __launch_bounds__(256, 2) k_group_nodes(LevelArgs a) {
+  constexpr int NPW = 32 / G;                 // nodes per warp
+  constexpr int NS = (10 + G - 1) / G;        // ERT samples per lane
   const int lane = threadIdx.x & 31;
+  const int gl = lane & (G - 1);
+  const int gi = lane / G;
+  const unsigned gm = G == 32 ? kFull : (((1u << G) - 1u) << (gi * G));
+  const unsigned glt = ((1u << lane) - 1u) & gm;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int wi = gw; wi < a.nwork; wi += nwarps) {
+  const int nslots = (a.nwork + NPW - 1) / NPW;
+  unsigned long long tries_done = 0;  // entry-tries evaluated (on group leaders)
+  for (int ws = gw; ws < nslots; ws += nwarps) {
+    const int wi = ws * NPW + gi;
+    if (wi >= a.nwork) continue;
     const int node = a.work[wi];
     const LNode nd = a.nodes[node];
     const ProbDesc& P = a.probs[nd.prob];
     const int C = P.C;
     const int m = nd.ecnt;
-    const bool valid = lane < m;
+    const bool valid = gl < m;
     const int* rows = a.rowsA + nd.ebeg;
     const int* ncnt = a.cnt + (long long)node * a.Cmax;
     const int ml = max(1, P.min_leaf);
-    const int row = valid ? __ldg(rows + lane) : 0;
-    const int w = valid ? (a.wA ? __ldg(a.wA + nd.ebeg + lane) : 1) : 0;
+    const int row = valid ? __ldg(rows + gl) : 0;
+    const int w = valid ? (a.wA ? __ldg(a.wA + nd.ebeg + gl) : 1) : 0;
     const int k = (valid && P.task == 0) ? __ldg(P.lab + row) : -1;
     const long long qv = (valid && P.task == 1) ? __ldg(P.q + row) : 0;
     ff prior{0.0f, 0.0f};
@@ -36,27 +66,32 @@ __global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
     if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     Cand best;
     best.valid = 0;
-    int bestL = 0;  // lane c holds the best split's left count of class c
     for (int t = 0;; ++t) {
       const int f = feature_of_try(P, nd, t);
       const float* xf = P.X + (long long)f * P.N;
       const float xv = valid ? __ldg(xf + row) : 0.0f;
       Cand cd;
       cd.f = f;
-      int myL = 0;
-      if (P.algo == 1) {  // ERT
-        float sv = 0.0f;
-        if (lane < 10) {
-          U4 r = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)(nd.tree + P.tree_key0),
-                       (uint32_t)nd.idx, (uint32_t)(t * 3 + lane / 4));
-          uint32_t pos = pick(r, lane & 3) % (uint32_t)m;
-          sv = __ldg(xf + __ldg(rows + pos));
+      if (P.algo == 1) {  // ERT: sample s is held by lane s % G, slot s / G
+        float sv[NS];
+#pragma unroll
+        for (int r = 0; r < NS; ++r) {
+          const int smp = gl + G * r;
+          sv[r] = 0.0f;
+          if (smp < 10) {
+            U4 rr = keyed(P.seed, kTagSample, (uint32_t)nd.depth, (uint32_t)(nd.tree + P.tree_key0),
+                          (uint32_t)nd.idx, (uint32_t)(t * 3 + smp / 4));
+            uint32_t pos = pick(rr, smp & 3) % (uint32_t)m;
+            sv[r] = __ldg(xf + __ldg(rows + pos));
+          }
         }
         float acc = 0.0f;
-        for (int s = 0; s < 10; ++s) acc = __fadd_rn(acc, __shfl_sync(kFull, sv, s));
+#pragma unroll
+        for (int smp = 0; smp < 10; ++smp)
+          acc = __fadd_rn(acc, __shfl_sync(gm, sv[smp / G], smp % G, G));
         const float thr = __fdiv_rn(acc, 10.0f);
         const bool left = valid && goes_left(xv, thr);
-        const unsigned lm = __ballot_sync(kFull, left);
+        const unsigned lm = __ballot_sync(gm, left);
         const long long nl = __popc(lm);
         const long long nr = (long long)nd.n - nl;
         cd.thr = thr;
@@ -65,31 +100,30 @@ __global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
         cd.suml = 0;
         cd.valid = nl >= ml && nr >= ml;
         if (P.task == 0) {
-          for (int c = 0; c < C; ++c) {
-            unsigned mc = __ballot_sync(kFull, k == c);
-            if (lane == c) myL = __popc(mc & lm);
-          }
-          cd.gain = cd.valid ? entropy_gain(
-                                   a.H, prior, C, nl, nr,
-                                   [&](int c) { return (long long)__shfl_sync(kFull, myL, c); },
-                                   [&](int c) { return (long long)ncnt[c]; })
+          int Lc[2 * CW];
+#pragma unroll
+          for (int c = 0; c < 2 * CW; ++c)
+            Lc[c] = c < C ? __popc(__ballot_sync(gm, k == c) & lm) : 0;
+          cd.gain = cd.valid ? entropy_gain_u<2 * CW>(
+                                   a.H, prior, C, nl, nr, [&](int c) { return (long long)Lc[c]; },
+                                   [&](int c) { return (long long)Nt[c]; })
                              : -FLT_MAX;
         } else {
-          long long sl = warp_sum<long long>(left ? qv : 0);
+          long long sl = grp_sum<G, long long>(left ? qv : 0, gm);
           cd.suml = sl;
           cd.gain = cd.valid ? variance_gain(nl, sl, nr, nd.sum - sl, P.S) : -FLT_MAX;
         }
-      } else {  // RF: bitonic sort of (key, lane)
+      } else {  // RF: bitonic sort of (key, lane) over the group
         uint32_t key = valid ? orderable(xv) : 0xFFFFFFFFu;
-        int idx = lane;
+        int idx = gl;
 #pragma unroll
-        for (int kk = 2; kk <= 32; kk <<= 1) {
+        for (int kk = 2; kk <= G; kk <<= 1) {
 #pragma unroll
           for (int j = kk >> 1; j > 0; j >>= 1) {
-            uint32_t pk = __shfl_xor_sync(kFull, key, j);
-            int pi = __shfl_xor_sync(kFull, idx, j);
-            bool up = (lane & kk) == 0;
-            bool lower = (lane & j) == 0;
+            uint32_t pk = __shfl_xor_sync(gm, key, j, G);
+            int pi = __shfl_xor_sync(gm, idx, j, G);
+            bool up = (gl & kk) == 0;
+            bool lower = (gl & j) == 0;
             bool mine_smaller = key < pk || (key == pk && idx < pi);
             bool keep = (lower == up) ? mine_smaller : !mine_smaller;
             if (!keep) {
@@ -98,63 +132,56 @@ __global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
             }
           }
         }
-        // lane p now holds sorted position p, originally lane idx
-        const int ke = __shfl_sync(kFull, k, idx);
-        const int we = __shfl_sync(kFull, w, idx);
-        const long long qe = __shfl_sync(kFull, qv, idx);
-        const float xe = __shfl_sync(kFull, xv, idx);
-        const uint32_t prevk = __shfl_up_sync(kFull, key, 1);
-        const float prevx = __shfl_up_sync(kFull, xe, 1);
-        const long long nl = warp_excl_scan<long long>(we);
+        // group lane p now holds sorted position p, originally group lane idx
+        const int ke = __shfl_sync(gm, k, idx, G);
+        const int we = __shfl_sync(gm, w, idx, G);
+        const long long qe = __shfl_sync(gm, qv, idx, G);
+        const float xe = __shfl_sync(gm, xv, idx, G);
+        const uint32_t prevk = __shfl_up_sync(gm, key, 1, G);
+        const float prevx = __shfl_up_sync(gm, xe, 1, G);
+        const long long nl = grp_excl_scan<G, long long>(we, gl, gm);
         const long long nr = (long long)nd.n - nl;
-        bool bnd = lane > 0 && lane < m && prevk < key && nl >= ml && nr >= ml;
+        bool bnd = gl > 0 && gl < m && prevk < key && nl >= ml && nr >= ml;
         float g = -FLT_MAX;
         long long sl = 0;
-        int L[2 * CW];
         if (P.task == 0) {
+          int L[2 * CW];
 #pragma unroll
           for (int c = 0; c < 2 * CW; ++c)
-            L[c] = c < C ? warp_excl_scan<int>(ke == c ? we : 0) : 0;
+            L[c] = c < C ? grp_excl_scan<G, int>(ke == c ? we : 0, gl, gm) : 0;
           if (bnd)
             g = entropy_gain_u<2 * CW>(
                 a.H, prior, C, nl, nr, [&](int c) { return (long long)L[c]; },
                 [&](int c) { return (long long)Nt[c]; });
         } else {
-          sl = warp_excl_scan<long long>(qe * (long long)we);
+          sl = grp_excl_scan<G, long long>(qe * (long long)we, gl, gm);
           if (bnd) g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
         }
-        // warp argmax: valid, higher gain, lower position
-        int bp = bnd ? lane : -1;
+        // group argmax: valid, higher gain, lower position
+        int bp = bnd ? gl : -1;
         float bg = g;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          float g2 = __shfl_xor_sync(kFull, bg, o);
-          int p2 = __shfl_xor_sync(kFull, bp, o);
+        for (int o = G / 2; o > 0; o >>= 1) {
+          float g2 = __shfl_xor_sync(gm, bg, o, G);
+          int p2 = __shfl_xor_sync(gm, bp, o, G);
           bool take = p2 >= 0 && (bp < 0 || g2 > bg || (g2 == bg && p2 < bp));
           if (take) {
             bg = g2;
             bp = p2;
           }
         }
+        const int src = bp >= 0 ? bp : 0;
+        const float xa = __shfl_sync(gm, prevx, src, G);
+        const float xb = __shfl_sync(gm, xe, src, G);
+        const long long nlb = __shfl_sync(gm, nl, src, G);
+        const long long slb = __shfl_sync(gm, sl, src, G);
         if (bp >= 0) {
           cd.valid = 1;
           cd.gain = bg;
-          float xa = __shfl_sync(kFull, prevx, bp);
-          float xb = __shfl_sync(kFull, xe, bp);
           cd.thr = midpoint_threshold(xa, xb);
           cd.nl_e = bp;
-          cd.nl = (int)__shfl_sync(kFull, nl, bp);
-          cd.suml = __shfl_sync(kFull, sl, bp);
-          if (P.task == 0) {
-            // lane c takes the class-c count of position bp
-            int mine = 0;
-#pragma unroll
-            for (int c = 0; c < 2 * CW; ++c) {
-              int v = __shfl_sync(kFull, L[c], bp);
-              if (lane == c) mine = v;
-            }
-            myL = mine;
-          }
+          cd.nl = (int)nlb;
+          cd.suml = slb;
         } else {
           cd.valid = 0;
           cd.gain = -FLT_MAX;
@@ -163,43 +190,43 @@ __global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
           cd.suml = 0;
         }
       }
-      // try-loop decision (uniform across the warp)
+      // try-loop decision (uniform across the group)
       bool more;
       if (t < P.n_mand) {
-        if (t == 0 || better(cd, best)) {
-          best = cd;
-          bestL = myL;
-        }
+        if (t == 0 || better(cd, best)) best = cd;
         more = (t + 1 < P.n_mand) || (P.n_opt > 0 && !(best.valid && best.gain >= kSensible));
       } else {
-        if (better(cd, best)) {
-          best = cd;
-          bestL = myL;
-        }
+        if (better(cd, best)) best = cd;
         more = !(cd.valid && cd.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
       }
       if (!more) {
-        if (lane == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)(t + 1) * m);
+        if (gl == 0) tries_done += (unsigned long long)(t + 1) * m;
         break;
       }
     }
     if (!best.valid) {
-      if (lane == 0) write_leaf(a.res, node);
+      if (gl == 0) write_leaf(a.res, node);
       continue;
     }
-    if (lane == 0) write_result(a.res, a.res_cnt, a.Cmax, node, best, nullptr, 0);
-    if (P.task == 0 && lane < C) a.res_cnt[(long long)node * a.Cmax + lane] = bestL;
-    // stable partition with one ballot
+    if (gl == 0) write_result(a.res, a.res_cnt, a.Cmax, node, best, nullptr, 0);
+    // stable partition with one ballot; the left class counts of the split
     const float xb = valid ? __ldg(P.X + (long long)best.f * P.N + row) : 0.0f;
     const bool left = valid && goes_left(xb, best.thr);
-    const unsigned lm = __ballot_sync(kFull, left);
+    const unsigned lm = __ballot_sync(gm, left);
+    if (P.task == 0)
+      for (int c = 0; c < C; ++c) {
+        const int lc = grp_sum<G, int>(left && k == c ? w : 0, gm);
+        if (gl == (c & (G - 1))) a.res_cnt[(long long)node * a.Cmax + c] = lc;
+      }
     if (valid) {
-      int pos = __popc(lm & lt);
-      long long dst = nd.ebeg + (left ? pos : best.nl_e + (lane - pos));
+      int pos = __popc(lm & glt);
+      long long dst = nd.ebeg + (left ? pos : best.nl_e + (gl - pos));
       a.rowsB[dst] = row;
       if (a.wB) a.wB[dst] = w;
     }
   }
+  tries_done = warp_sum<unsigned long long>(tries_done);
+  if (lane == 0 && tries_done) atomicAdd((unsigned long long*)&a.stats[2], tries_done);
 }
 
 // ============================================================ work queues
@@ -207,7 +234,7 @@ __global__ void __launch_bounds__(256, 2) k_warp_nodes(LevelArgs a) {
 // memory sort), RF big (CTA, global sort).  Queue order does not affect
 // results, only scheduling.
 enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kQRfW2 = 4, kQRfW4 = 5, kQRfW8 = 6,
-       kQRfW16 = 7, kNumQ = 8 };
+       kQG16 = 7, kQG8 = 8, kNumQ = 9 };
 
 struct Queues {
   int* list[kNumQ];
@@ -231,6 +258,8 @@ __device__ __forceinline__ void enqueue(Queues Q, int q, int node, bool want) {
 }
 
 __device__ __forceinline__ int queue_of(const ProbDesc& P, int ecnt, int small_cap) {
+  if (ecnt <= 8) return kQG8;
+  if (ecnt <= 16) return kQG16;
   if (ecnt <= 32) return kQWarp;
   if (P.algo == 1) return kQErt;
   if (ecnt <= 64) return kQRfW2;

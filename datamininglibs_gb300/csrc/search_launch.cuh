@@ -34,14 +34,17 @@ void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s) {
   b.nwork = count;
   const int wblocks = std::max(1, std::min((count + 7) / 8, 1 << 20));
   if (q == kQWarp) {
-    k_warp_nodes<CW><<<wblocks, 256, 0, s>>>(b);
+    k_group_nodes<CW, 32><<<wblocks, 256, 0, s>>>(b);
+  } else if (q == kQG16) {
+    k_group_nodes<CW, 16><<<std::max(1, std::min((count + 15) / 16, 1 << 20)), 256, 0, s>>>(b);
+  } else if (q == kQG8) {
+    k_group_nodes<CW, 8><<<std::max(1, std::min((count + 31) / 32, 1 << 20)), 256, 0, s>>>(b);
   } else if (q == kQRfW2) {
     k_warp_rf<2, CW><<<wblocks, 256, 0, s>>>(b);
   } else if (q == kQRfW4) {
     k_warp_rf<4, CW><<<wblocks, 256, 0, s>>>(b);
   } else if (q == kQRfW8) {
     k_warp_rf<8, CW><<<wblocks, 256, 0, s>>>(b);
-
   } else if (q == kQErt) {
     k_ert_cta<kBlock><<<std::min(count, 1 << 20), kBlock, 0, s>>>(b);
   } else {
