@@ -58,6 +58,28 @@ __global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict_
   }
 }
 
+// The reference's predict structure (gpudte.cu:311-359): one thread per
+// (tree, row) of one tree; votes are added to the output (a launch holds each
+// row once, so plain adds keep tree order).
+template <int TASK>
+__global__ void k_predict_plain(const PNode* __restrict__ nodes, int tree, int C,
+                                const float* __restrict__ X, long long N, long long row0,
+                                long long rows, float* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  const long long row = row0 + i;
+  int4 p = __ldg(reinterpret_cast<const int4*>(nodes) + tree);
+  while (p.x >= 0) {
+    float x = __ldg(X + (long long)p.y * N + row);
+    int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
+    p = __ldg(reinterpret_cast<const int4*>(nodes) + nx);
+  }
+  if (TASK == 0)
+    out[row * C + p.y] = __fadd_rn(out[row * C + p.y], 1.0f);
+  else
+    out[row] = __fadd_rn(out[row], __int_as_float(p.z));
+}
+
 dml_status predict_device(const dml_forest* f, const float* dX, long long n_rows, float* dout,
                           cudaStream_t s) {
   if (n_rows <= 0) return DML_OK;
@@ -126,6 +148,67 @@ dml_status dml_predict(const dml_forest* f, const float* samples, int64_t n_rows
   if (st == DML_OK && e != cudaSuccess) {
     set_error("predict failed: %s", cudaGetErrorString(e));
     st = DML_ERR_CUDA;
+  }
+  return st;
+}
+
+dml_status dml_predict_plain(const dml_forest* f, const float* samples, int64_t n_rows,
+                             float* out, int32_t memory, void* stream) {
+  clear_error();
+  if (!f || (!samples && n_rows > 0) || (!out && n_rows > 0) || n_rows < 0 ||
+      (memory != DML_HOST && memory != DML_DEVICE)) {
+    set_error("invalid predict arguments");
+    return DML_ERR_INVALID_ARG;
+  }
+  if (n_rows == 0) return DML_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long width = f->task == DML_CLASSIFICATION ? f->n_classes : 1;
+  const size_t xb = sizeof(float) * (size_t)n_rows * f->n_features;
+  const size_t ob = sizeof(float) * (size_t)n_rows * width;
+  init_pool_once();
+  const float* dX = samples;
+  float* dout = out;
+  float* tX = nullptr;
+  float* tout = nullptr;
+  if (memory == DML_HOST) {  // AllocatePredict's uploads (gpudte_algorithm.cc:639-673)
+    if (cudaMallocAsync(&tX, xb, s) != cudaSuccess || cudaMallocAsync(&tout, ob, s) != cudaSuccess) {
+      cudaGetLastError();
+      if (tX) cudaFreeAsync(tX, s);
+      set_error("device allocation failed for a predict of %lld rows", (long long)n_rows);
+      return DML_ERR_OOM;
+    }
+    cudaMemcpyAsync(tX, samples, xb, cudaMemcpyHostToDevice, s);
+    dX = tX;
+    dout = tout;
+  }
+  dml_status st = DML_OK;
+  cudaMemsetAsync(dout, 0, ob, s);
+  // at most 65,536 (tree, row) threads per launch, a sync after each
+  // (gpudte_algorithm.cc:292-311)
+  constexpr long long kChunk = 65536;
+  for (int t = 0; t < f->n_trees && st == DML_OK; ++t)
+    for (long long r0 = 0; r0 < n_rows && st == DML_OK; r0 += kChunk) {
+      const long long rows = std::min<long long>(kChunk, n_rows - r0);
+      const unsigned blocks = (unsigned)((rows + 63) / 64);
+      if (f->task == DML_CLASSIFICATION)
+        k_predict_plain<0><<<blocks, 64, 0, s>>>(f->pnodes, t, f->n_classes, dX, n_rows, r0, rows,
+                                                 dout);
+      else
+        k_predict_plain<1><<<blocks, 64, 0, s>>>(f->pnodes, t, 1, dX, n_rows, r0, rows, dout);
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        set_error("predict failed: %s", cudaGetErrorString(e));
+        st = DML_ERR_CUDA;
+      }
+    }
+  if (memory == DML_HOST) {
+    if (st == DML_OK && cudaMemcpyAsync(out, tout, ob, cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+      set_error("device to host copy failed");
+      st = DML_ERR_CUDA;
+    }
+    cudaFreeAsync(tX, s);
+    cudaFreeAsync(tout, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess && st == DML_OK) st = DML_ERR_CUDA;
   }
   return st;
 }

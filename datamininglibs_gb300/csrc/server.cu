@@ -2,19 +2,26 @@
 // admission.  No reference counterpart (the reference predicts one data frame
 // per call, gpudte_algorithm.cc:270-331).
 //
-// A worker thread keeps up to n_streams batches in flight.  A batch packs the
-// queued requests (any mix of forests) that fit the batch-row limit and the
-// free part of the device budget into one launch over a list of 128-row
-// tiles; each tile walks its request's forest for its rows.  Requests that
-// arrive while batches run join the next batch as soon as a stream slot and
-// budget free up.  Request rows are staged through pinned host memory; results
-// are copied back to the caller's buffer when the batch's event completes.
+// One worker thread drives two lanes, each with n_streams batch slots:
+//  * small lane (requests of at most small_rows rows): high-priority streams;
+//    a batch packs whole requests of any forests into 16-row tiles whose rows
+//    are walked by 8 threads each (one eighth of the trees per thread), which
+//    cuts a row's chain of dependent node loads by 8;
+//  * large lane: low-priority streams; requests are cut into slices of at most
+//    max_batch_rows rows and a batch packs slices into 128-row tiles (one
+//    thread per row walks every tree).
+// Blocks of a low-priority launch are short (one tile), so a small batch waits
+// for at most one block per SM.  Requests that arrive while batches run join
+// the next batch of their lane as soon as a slot and budget free up.  Pinned
+// host buffers are copied by DMA; pageable ones are staged through pinned
+// slot buffers.  A request completes when all of its rows are back.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -31,18 +38,22 @@ void init_pool_once();
 
 namespace {
 
-constexpr int kTileRows = 128;
+constexpr int kTileRows = 128;      // large lane: rows per tile (one thread per row)
+constexpr int kSplit = 8;           // small lane: threads per row
+constexpr int kSplitRows = kTileRows / kSplit;
+constexpr int kSplitMaxTrees = 512;  // small-lane regression keeps [rows][trees] leaf values
 
 struct PredTile {
   const PNode* nodes;
-  const float* X;   // feature-major rows of the request: X[f * n + i]
+  const float* X;   // feature-major rows of the slice: X[f * n + i]
   float* out;       // [n * width]
-  long long n;      // rows of the request
+  long long n;      // rows of the slice
   int row0, rows;   // this tile
   int n_trees, C, task, pad;
 };
 
-template <int UNUSED>
+// Large lane: a thread walks every tree for its row (tree order, so regression
+// sums match dml_predict bit for bit).
 __global__ void __launch_bounds__(kTileRows) k_predict_tiles(const PredTile* __restrict__ tiles) {
   extern __shared__ int votes[];  // [kTileRows][C]
   const PredTile t = tiles[blockIdx.x];
@@ -73,6 +84,47 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles(const PredTile* __r
   }
 }
 
+// Small lane: 8 threads per row, thread g walks trees g, g+8, ...; votes meet
+// in shared memory (integer counts, order-free); regression leaf values are
+// kept per tree and summed in tree order by one thread.
+__global__ void __launch_bounds__(kTileRows) k_predict_tiles_split(
+    const PredTile* __restrict__ tiles) {
+  extern __shared__ int sm[];  // votes [kSplitRows][C] or values [kSplitRows][n_trees]
+  const PredTile t = tiles[blockIdx.x];
+  const int g = threadIdx.x % kSplit;
+  const int r = threadIdx.x / kSplit;
+  const bool act = r < t.rows;
+  const long long row = (long long)t.row0 + r;
+  if (t.task == 0)
+    for (int i = threadIdx.x; i < kSplitRows * t.C; i += kTileRows) sm[i] = 0;
+  __syncthreads();
+  float* vals = reinterpret_cast<float*>(sm) + r * t.n_trees;
+  if (act) {
+    for (int k = g; k < t.n_trees; k += kSplit) {
+      int4 p = __ldg(reinterpret_cast<const int4*>(t.nodes) + k);
+      while (p.x >= 0) {
+        const float x = __ldg(t.X + (long long)p.y * t.n + row);
+        const int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
+        p = __ldg(reinterpret_cast<const int4*>(t.nodes) + nx);
+      }
+      if (t.task == 0)
+        atomicAdd(&sm[r * t.C + p.y], 1);
+      else
+        vals[k] = __int_as_float(p.z);
+    }
+  }
+  __syncthreads();
+  if (act) {
+    if (t.task == 0) {
+      for (int c = g; c < t.C; c += kSplit) t.out[row * t.C + c] = (float)sm[r * t.C + c];
+    } else if (g == 0) {
+      float acc = 0.0f;
+      for (int k = 0; k < t.n_trees; ++k) acc = __fadd_rn(acc, vals[k]);
+      t.out[row] = acc;
+    }
+  }
+}
+
 using Clock = std::chrono::steady_clock;
 
 struct Request {
@@ -82,13 +134,20 @@ struct Request {
   long long n;
   float* out;
   Clock::time_point t_submit;
-  size_t in_bytes, out_bytes;
+  int width, n_features;
+  bool pinned_in, pinned_out;
+  long long next_row = 0;   // first row not yet handed to a batch
+  long long rows_left = 0;  // rows not yet completed
+};
+
+struct Piece {  // rows [row0, row0 + rows) of a request in a batch
+  std::shared_ptr<Request> req;
+  long long row0, rows;
+  size_t in_off, out_off;
 };
 
 struct Batch {
-  std::vector<Request> reqs;
-  std::vector<size_t> in_off, out_off;  // offsets in the slot's staging buffers
-  size_t bytes = 0;
+  std::vector<Piece> pieces;
   cudaEvent_t done = nullptr;
   bool busy = false;
 };
@@ -101,8 +160,9 @@ struct Slot {
   char* d_out = nullptr;
   PredTile* d_tiles = nullptr;
   PredTile* h_tiles = nullptr;
-  size_t cap = 0;         // bytes of each staging direction
+  size_t cap = 0;         // bytes of each direction
   int tile_cap = 0;
+  bool small = false;
   Batch batch;
 };
 
@@ -112,28 +172,38 @@ struct Slot {
 struct dml_server {
   dml_server_config cfg;
   int device = 0;
+  long long small_rows = 4096;
   std::vector<const dml_forest*> forests;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<dml::Request> queue;
+  std::deque<std::shared_ptr<dml::Request>> q_small, q_large;
   std::unordered_map<long long, double> done;  // id -> latency ms
   std::vector<double> latencies;
   long long next_id = 1, completed = 0, rows = 0, launches = 0, rejected = 0;
   dml::Clock::time_point first_submit, last_done;
   bool have_first = false, stop = false;
-  std::vector<dml::Slot> slots;
+  std::vector<dml::Slot> slots;  // n_streams small-lane slots, then n_streams large-lane
   std::thread worker;
-  size_t budget_per_slot = 0;
+  size_t small_cap = 0, large_cap = 0;
 };
 
 namespace dml {
 namespace {
 
-size_t req_in_bytes(const dml_forest* f, long long n) { return sizeof(float) * (size_t)n * f->n_features; }
-size_t req_out_bytes(const dml_forest* f, long long n) {
-  return sizeof(float) * (size_t)n * (f->task == DML_CLASSIFICATION ? f->n_classes : 1);
-}
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+bool split_ok(const dml_forest* f) {
+  return f->task == DML_CLASSIFICATION || f->n_trees <= kSplitMaxTrees;
+}
 
 // Completes finished batches; returns true if any slot finished.
 bool reap(dml_server* s) {
@@ -141,91 +211,129 @@ bool reap(dml_server* s) {
   for (Slot& sl : s->slots) {
     if (!sl.batch.busy) continue;
     if (cudaEventQuery(sl.batch.done) != cudaSuccess) continue;
-    for (size_t i = 0; i < sl.batch.reqs.size(); ++i) {
-      const Request& r = sl.batch.reqs[i];
-      std::memcpy(r.out, sl.h_out + sl.batch.out_off[i], r.out_bytes);
+    for (const Piece& p : sl.batch.pieces) {
+      const Request& r = *p.req;
+      if (!r.pinned_out)
+        std::memcpy(r.out + p.row0 * r.width, sl.h_out + p.out_off,
+                    sizeof(float) * p.rows * r.width);
     }
     auto now = Clock::now();
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      for (const Request& r : sl.batch.reqs) {
-        double ms = std::chrono::duration<double, std::milli>(now - r.t_submit).count();
-        s->done[r.id] = ms;
-        s->latencies.push_back(ms);
-        s->completed++;
-        s->rows += r.n;
+      for (const Piece& p : sl.batch.pieces) {
+        Request& r = *p.req;
+        r.rows_left -= p.rows;
+        if (r.rows_left == 0) {
+          double ms = std::chrono::duration<double, std::milli>(now - r.t_submit).count();
+          s->done[r.id] = ms;
+          s->latencies.push_back(ms);
+          s->completed++;
+          s->rows += r.n;
+        }
       }
       s->last_done = now;
     }
     s->cv_done.notify_all();
-    sl.batch.reqs.clear();
+    sl.batch.pieces.clear();
     sl.batch.busy = false;
     any = true;
   }
   return any;
 }
 
-// Packs queued requests into a free slot and launches the batch.
+// Packs queued work of the slot's lane into the slot and launches it.
 bool launch_batch(dml_server* s, Slot& sl) {
   Batch& b = sl.batch;
-  b.reqs.clear();
-  b.in_off.clear();
-  b.out_off.clear();
+  b.pieces.clear();
+  const int tile_rows = sl.small ? kSplitRows : kTileRows;
+  const long long max_rows = sl.small ? std::max<long long>(s->small_rows * 16, 65536)
+                                      : s->cfg.max_batch_rows;
   size_t in_used = 0, out_used = 0;
   long long rows = 0;
   int tiles = 0;
   {
     std::lock_guard<std::mutex> lk(s->mu);
-    while (!s->queue.empty()) {
-      const Request& r = s->queue.front();
-      const int rt = (int)((r.n + kTileRows - 1) / kTileRows);
-      if (!b.reqs.empty() && (rows + r.n > s->cfg.max_batch_rows ||
-                              in_used + align256(r.in_bytes) > sl.cap ||
-                              out_used + align256(r.out_bytes) > sl.cap || tiles + rt > sl.tile_cap))
-        break;
-      if (b.reqs.empty() && (align256(r.in_bytes) > sl.cap || align256(r.out_bytes) > sl.cap ||
-                             rt > sl.tile_cap))
-        break;  // cannot happen: rejected at submit
-      b.in_off.push_back(in_used);
-      b.out_off.push_back(out_used);
-      in_used += align256(r.in_bytes);
-      out_used += align256(r.out_bytes);
-      rows += r.n;
-      tiles += rt;
-      b.reqs.push_back(r);
-      s->queue.pop_front();
+    auto& q = sl.small ? s->q_small : s->q_large;
+    while (!q.empty() && rows < max_rows) {
+      std::shared_ptr<Request> r = q.front();
+      const long long row_in = (long long)sizeof(float) * r->n_features;
+      const long long row_out = (long long)sizeof(float) * r->width;
+      // rows of this request that fit the batch's remaining room (64 rows of
+      // slack cover the 256-byte alignment of each piece)
+      long long room = max_rows - rows;
+      room = std::min(room, (long long)(sl.cap - in_used) / row_in - 64);
+      room = std::min(room, (long long)(sl.cap - out_used) / row_out - 64);
+      room = std::min(room, (long long)(sl.tile_cap - tiles) * tile_rows);
+      const long long want = r->n - r->next_row;
+      if (room <= 0 || (sl.small && room < want)) break;  // small requests are not split
+      const long long take = std::min(want, room);
+      Piece p{r, r->next_row, take, in_used, out_used};
+      in_used += align256(row_in * take);
+      out_used += align256(row_out * take);
+      rows += take;
+      tiles += (int)((take + tile_rows - 1) / tile_rows);
+      r->next_row += take;
+      if (r->next_row == r->n) q.pop_front();
+      b.pieces.push_back(std::move(p));
     }
   }
-  if (b.reqs.empty()) return false;
+  if (b.pieces.empty()) return false;
+  cudaStream_t st = sl.stream;
   int nt = 0;
-  for (size_t i = 0; i < b.reqs.size(); ++i) {
-    const Request& r = b.reqs[i];
+  int shm = sizeof(int);
+  for (const Piece& p : b.pieces) {
+    const Request& r = *p.req;
     const dml_forest* f = s->forests[r.forest];
-    std::memcpy(sl.h_in + b.in_off[i], r.samples, r.in_bytes);
-    for (long long r0 = 0; r0 < r.n; r0 += kTileRows) {
+    char* d_x = sl.d_in + p.in_off;
+    const size_t rb = sizeof(float) * p.rows;
+    if (r.pinned_in) {
+      if (p.rows == r.n)
+        cudaMemcpyAsync(d_x, r.samples, rb * r.n_features, cudaMemcpyHostToDevice, st);
+      else
+        cudaMemcpy2DAsync(d_x, rb, r.samples + p.row0, sizeof(float) * r.n, rb, r.n_features,
+                          cudaMemcpyHostToDevice, st);
+    } else {
+      char* h = sl.h_in + p.in_off;
+      if (p.rows == r.n)
+        std::memcpy(h, r.samples, rb * r.n_features);
+      else
+        for (int j = 0; j < r.n_features; ++j)
+          std::memcpy(h + rb * j, r.samples + (long long)j * r.n + p.row0, rb);
+      cudaMemcpyAsync(d_x, h, rb * r.n_features, cudaMemcpyHostToDevice, st);
+    }
+    for (long long r0 = 0; r0 < p.rows; r0 += tile_rows) {
       PredTile& t = sl.h_tiles[nt++];
       t.nodes = f->pnodes;
-      t.X = (const float*)(sl.d_in + b.in_off[i]);
-      t.out = (float*)(sl.d_out + b.out_off[i]);
-      t.n = r.n;
+      t.X = (const float*)d_x;
+      t.out = (float*)(sl.d_out + p.out_off);
+      t.n = p.rows;
       t.row0 = (int)r0;
-      t.rows = (int)std::min<long long>(kTileRows, r.n - r0);
+      t.rows = (int)std::min<long long>(tile_rows, p.rows - r0);
       t.n_trees = f->n_trees;
-      t.C = f->task == DML_CLASSIFICATION ? f->n_classes : 1;
+      t.C = r.width;
       t.task = f->task;
       t.pad = 0;
     }
+    const int need = sl.small ? (f->task == DML_CLASSIFICATION ? kSplitRows * r.width
+                                                               : kSplitRows * f->n_trees)
+                              : (f->task == DML_CLASSIFICATION ? kTileRows * r.width : 1);
+    shm = std::max(shm, (int)sizeof(int) * need);
   }
-  cudaMemcpyAsync(sl.d_in, sl.h_in, in_used, cudaMemcpyHostToDevice, sl.stream);
-  cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, sizeof(PredTile) * nt, cudaMemcpyHostToDevice, sl.stream);
-  int Cmax = 1;
-  for (const Request& r : b.reqs) {
-    const dml_forest* f = s->forests[r.forest];
-    if (f->task == DML_CLASSIFICATION) Cmax = std::max(Cmax, f->n_classes);
+  cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, sizeof(PredTile) * nt, cudaMemcpyHostToDevice, st);
+  if (sl.small)
+    k_predict_tiles_split<<<nt, kTileRows, shm, st>>>(sl.d_tiles);
+  else
+    k_predict_tiles<<<nt, kTileRows, shm, st>>>(sl.d_tiles);
+  for (const Piece& p : b.pieces) {
+    const Request& r = *p.req;
+    const size_t ob = sizeof(float) * p.rows * r.width;
+    if (r.pinned_out)
+      cudaMemcpyAsync(r.out + p.row0 * r.width, sl.d_out + p.out_off, ob, cudaMemcpyDeviceToHost,
+                      st);
+    else
+      cudaMemcpyAsync(sl.h_out + p.out_off, sl.d_out + p.out_off, ob, cudaMemcpyDeviceToHost, st);
   }
-  k_predict_tiles<0><<<nt, kTileRows, sizeof(int) * kTileRows * Cmax, sl.stream>>>(sl.d_tiles);
-  cudaMemcpyAsync(sl.h_out, sl.d_out, out_used, cudaMemcpyDeviceToHost, sl.stream);
-  cudaEventRecord(b.done, sl.stream);
+  cudaEventRecord(b.done, st);
   b.busy = true;
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -238,39 +346,40 @@ void worker_main(dml_server* s) {
   cudaSetDevice(s->device);
   while (true) {
     bool progressed = reap(s);
-    bool have_free = false;
+    bool small_idle = true;
     for (Slot& sl : s->slots)
-      if (!sl.batch.busy) {
-        have_free = true;
-        bool pending;
-        {
-          std::lock_guard<std::mutex> lk(s->mu);
-          pending = !s->queue.empty();
-        }
-        if (!pending) break;
-        if (s->cfg.max_wait_us > 0) {
-          // let a batch fill briefly when the GPU is idle and few rows wait
-          std::unique_lock<std::mutex> lk(s->mu);
-          long long waiting = 0;
-          for (const Request& r : s->queue) waiting += r.n;
-          bool idle = true;
-          for (Slot& o : s->slots) idle = idle && !o.batch.busy;
-          if (idle && waiting < s->cfg.max_batch_rows / 8)
-            s->cv_work.wait_for(lk, std::chrono::microseconds(s->cfg.max_wait_us));
-        }
-        progressed |= launch_batch(s, sl);
+      if (sl.small) small_idle = small_idle && !sl.batch.busy;
+    for (Slot& sl : s->slots) {
+      if (sl.batch.busy) continue;
+      bool pending;
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        pending = !(sl.small ? s->q_small : s->q_large).empty();
       }
+      if (!pending) continue;
+      if (sl.small && small_idle && s->cfg.max_wait_us > 0) {
+        // an idle lane lets a batch fill briefly while few rows wait
+        std::unique_lock<std::mutex> lk(s->mu);
+        long long waiting = 0;
+        for (auto& r : s->q_small) waiting += r->n - r->next_row;
+        if (waiting < s->small_rows)
+          s->cv_work.wait_for(lk, std::chrono::microseconds(s->cfg.max_wait_us));
+        small_idle = false;
+      }
+      progressed |= launch_batch(s, sl);
+    }
     bool any_busy = false;
     for (Slot& sl : s->slots) any_busy |= sl.batch.busy;
     std::unique_lock<std::mutex> lk(s->mu);
-    if (s->stop && s->queue.empty() && !any_busy) break;
+    const bool queued = !s->q_small.empty() || !s->q_large.empty();
+    if (s->stop && !queued && !any_busy) break;
     if (!progressed) {
-      if (any_busy || (!s->queue.empty() && !have_free)) {
+      if (any_busy) {
         lk.unlock();
-        std::this_thread::sleep_for(std::chrono::microseconds(20));
+        std::this_thread::sleep_for(std::chrono::microseconds(10));
       } else {
         s->cv_work.wait_for(lk, std::chrono::milliseconds(5),
-                            [&] { return s->stop || !s->queue.empty(); });
+                            [&] { return s->stop || !s->q_small.empty() || !s->q_large.empty(); });
       }
     }
   }
@@ -286,24 +395,34 @@ extern "C" {
 dml_status dml_server_create(const dml_server_config* cfg, dml_server** out) {
   clear_error();
   if (!cfg || !out || cfg->hbm_budget_bytes <= 0 || cfg->max_batch_rows <= 0 ||
-      cfg->n_streams <= 0 || cfg->n_streams > 64 || cfg->max_wait_us < 0) {
+      cfg->n_streams <= 0 || cfg->n_streams > 32 || cfg->max_wait_us < 0 || cfg->small_rows < 0) {
     set_error("invalid server configuration");
     return DML_ERR_INVALID_ARG;
   }
   init_pool_once();
   dml_server* s = new dml_server();
   s->cfg = *cfg;
+  s->small_rows = cfg->small_rows > 0 ? cfg->small_rows : 4096;
   cudaGetDevice(&s->device);
-  s->slots.resize(cfg->n_streams);
-  // half of a slot's share of the budget for inputs, half for outputs
-  s->budget_per_slot = (size_t)(cfg->hbm_budget_bytes / cfg->n_streams / 2) & ~(size_t)255;
-  bool ok = s->budget_per_slot >= 4096;
-  for (Slot& sl : s->slots) {
-    if (!ok) break;
-    sl.cap = s->budget_per_slot;
+  int prio_low = 0, prio_high = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  // a quarter of the budget for the small lane, the rest for the large lane;
+  // each slot's share is split between inputs and outputs
+  const int ns = cfg->n_streams;
+  s->small_cap = (size_t)(cfg->hbm_budget_bytes / 4 / ns / 2) & ~(size_t)255;
+  s->large_cap = (size_t)(cfg->hbm_budget_bytes * 3 / 4 / ns / 2) & ~(size_t)255;
+  s->slots.resize(2 * ns);
+  bool ok = s->small_cap >= (1 << 16) && s->large_cap >= (1 << 16);
+  for (int i = 0; i < 2 * ns && ok; ++i) {
+    Slot& sl = s->slots[i];
+    sl.small = i < ns;
+    sl.cap = sl.small ? s->small_cap : s->large_cap;
+    const long long lane_rows = sl.small ? std::max<long long>(s->small_rows * 16, 65536)
+                                         : cfg->max_batch_rows;
     sl.tile_cap = (int)std::min<long long>(
-        1 << 22, cfg->max_batch_rows / kTileRows + 4 * 1024);
-    ok = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
+        1 << 22, lane_rows / (sl.small ? kSplitRows : kTileRows) + 1024);
+    ok = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking,
+                                      sl.small ? prio_high : prio_low) == cudaSuccess &&
          cudaMallocHost(&sl.h_in, sl.cap) == cudaSuccess &&
          cudaMallocHost(&sl.h_out, sl.cap) == cudaSuccess &&
          cudaMallocHost(&sl.h_tiles, sizeof(PredTile) * sl.tile_cap) == cudaSuccess &&
@@ -338,11 +457,12 @@ dml_status dml_server_add_forest(dml_server* s, const dml_forest* forest, int32_
 dml_status dml_server_submit(dml_server* s, int32_t forest_id, const float* samples,
                              int64_t n_rows, float* out, int64_t* request_id) {
   clear_error();
-  if (!s || !samples || !out || !request_id || n_rows <= 0 || n_rows > (1 << 20)) {
-    set_error("invalid request (rows must be in 1 .. 1048576)");
+  if (!s || !samples || !out || !request_id || n_rows <= 0 || n_rows > (1LL << 31)) {
+    set_error("invalid request");
     return DML_ERR_INVALID_ARG;
   }
-  Request r;
+  auto r = std::make_shared<Request>();
+  const bool pin_in = is_pinned(samples), pin_out = is_pinned(out);
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (forest_id < 0 || forest_id >= (int32_t)s->forests.size()) {
@@ -350,26 +470,34 @@ dml_status dml_server_submit(dml_server* s, int32_t forest_id, const float* samp
       return DML_ERR_INVALID_ARG;
     }
     const dml_forest* f = s->forests[forest_id];
-    r.in_bytes = req_in_bytes(f, n_rows);
-    r.out_bytes = req_out_bytes(f, n_rows);
-    if (align256(r.in_bytes) > s->budget_per_slot || align256(r.out_bytes) > s->budget_per_slot ||
-        n_rows > s->cfg.max_batch_rows) {
+    r->width = f->task == DML_CLASSIFICATION ? f->n_classes : 1;
+    r->n_features = f->n_features;
+    // admission: a small request must fit a small slot whole; a large one is
+    // sliced, and a slice of 128 rows must fit a large slot
+    const size_t row_in = sizeof(float) * f->n_features, row_out = sizeof(float) * r->width;
+    const bool small_fit = n_rows <= s->small_rows && split_ok(f) &&
+                           align256(row_in * n_rows) + 64 * row_in <= s->small_cap &&
+                           align256(row_out * n_rows) + 64 * row_out <= s->small_cap;
+    if (!small_fit && (192 * row_in > s->large_cap || 192 * row_out > s->large_cap)) {
       s->rejected++;
-      set_error("request of %lld rows exceeds the server's per-batch budget", (long long)n_rows);
+      set_error("a row of forest %d does not fit the server's device budget", forest_id);
       return DML_ERR_BUDGET;
     }
-    r.id = s->next_id++;
-    r.forest = forest_id;
-    r.samples = samples;
-    r.n = n_rows;
-    r.out = out;
-    r.t_submit = Clock::now();
+    r->id = s->next_id++;
+    r->forest = forest_id;
+    r->samples = samples;
+    r->n = n_rows;
+    r->out = out;
+    r->pinned_in = pin_in;
+    r->pinned_out = pin_out;
+    r->rows_left = n_rows;
+    r->t_submit = Clock::now();
     if (!s->have_first) {
-      s->first_submit = r.t_submit;
+      s->first_submit = r->t_submit;
       s->have_first = true;
     }
-    s->queue.push_back(r);
-    *request_id = r.id;
+    (small_fit ? s->q_small : s->q_large).push_back(r);
+    *request_id = r->id;
   }
   s->cv_work.notify_one();
   return DML_OK;

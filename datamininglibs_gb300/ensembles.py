@@ -63,7 +63,7 @@ class FitStats(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch_rows", ctypes.c_int32),
                 ("n_streams", ctypes.c_int32), ("max_wait_us", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("small_rows", ctypes.c_int32)]
 
 
 class ServerStats(ctypes.Structure):
@@ -90,6 +90,8 @@ _SIGS = {
                                        ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
     "dml_predict": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                    ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "dml_predict_plain": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                         ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
     "dml_forest_info_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForestInfo)]),
     "dml_forest_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "dml_forest_import": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
@@ -181,6 +183,14 @@ class Forest:
     def predict(self, X, out=None, stream=None):
         """X feature-major [F, N] (numpy or CUDA tensor).  Returns the
         [N, C] vote counts (classification) or [N, 1] sums (regression)."""
+        return self._predict(lib().dml_predict, X, out, stream)
+
+    def predict_plain(self, X, out=None, stream=None):
+        """The same votes through the reference's launch structure
+        (dml_predict_plain): the baseline of the serving speed-up."""
+        return self._predict(lib().dml_predict_plain, X, out, stream)
+
+    def _predict(self, fn, X, out, stream):
         i = self.info()
         width = i.n_classes if i.task == CLASSIFICATION else 1
         n = X.shape[1]
@@ -194,7 +204,7 @@ class Forest:
         op, omem = _ptr(out)
         if omem != mem:
             raise ValueError("X and out must both be host or both device memory")
-        _check(lib().dml_predict(self._h, xp, n, op, mem, _stream(stream)))
+        _check(fn(self._h, xp, n, op, mem, _stream(stream)))
         return out
 
     def free(self):
@@ -307,9 +317,9 @@ def accuracy(votes, targets):
 class Server:
     """Resident-forest prediction server with continuous batching (dml_server_*)."""
 
-    def __init__(self, hbm_budget_bytes=8 << 30, max_batch_rows=1 << 20, n_streams=4,
-                 max_wait_us=100):
-        cfg = ServerConfig(hbm_budget_bytes, max_batch_rows, n_streams, max_wait_us, 0)
+    def __init__(self, hbm_budget_bytes=8 << 30, max_batch_rows=1 << 16, n_streams=4,
+                 max_wait_us=100, small_rows=4096):
+        cfg = ServerConfig(hbm_budget_bytes, max_batch_rows, n_streams, max_wait_us, small_rows)
         h = ctypes.c_void_p()
         _check(lib().dml_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

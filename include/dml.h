@@ -150,6 +150,15 @@ DML_API dml_status dml_last_fit_stats(dml_fit_stats* stats);
 DML_API dml_status dml_predict(const dml_forest* forest, const float* samples, int64_t n_rows,
                                float* out, int32_t memory, void* stream);
 
+/* The same votes with the reference's predict launch structure
+ * (gpudte_algorithm.cc:292-311, gpudte.cu:311-359): one thread per (tree, row),
+ * at most 65,536 threads per launch, a host sync after every launch, and host
+ * samples copied in and votes copied out on every call.  Launches cover one
+ * tree at a time, so sums keep tree order and equal dml_predict's.  The
+ * denominator of the serving speed-up; not a fast path. */
+DML_API dml_status dml_predict_plain(const dml_forest* forest, const float* samples,
+                                     int64_t n_rows, float* out, int32_t memory, void* stream);
+
 DML_API dml_status dml_forest_info_get(const dml_forest* forest, dml_forest_info* info);
 
 /* The model slots kNodeArray / kProbArray (lib_models/include/models_interface.h:9-19,
@@ -176,17 +185,22 @@ DML_API dml_status dml_set_device(int32_t device);
 
 /* ------------------------------------------------------------------ serving
  * No reference counterpart (the reference has no serving path): a resident-
- * forest prediction server with continuous batching.  Requests of 1..65536 rows
- * are admitted while earlier ones run, as HBM budget and batch slots free up;
- * their work shares kernel launches across streams. */
+ * forest prediction server with continuous batching.  Requests are admitted
+ * while earlier ones run, as HBM budget and batch slots free up; their work
+ * shares kernel launches across streams.  Two lanes: requests of at most
+ * small_rows rows run on high-priority streams with the trees of a row split
+ * over 8 threads (latency); larger requests run on low-priority streams in
+ * slices of at most max_batch_rows rows (throughput), so a large request never
+ * holds the device for long.  Host buffers that are pinned (cudaHostAlloc /
+ * cudaHostRegister) are copied by DMA directly; others are staged. */
 typedef struct dml_server dml_server;
 
 typedef struct {
   int64_t hbm_budget_bytes;   /* device bytes for request inputs/outputs */
-  int32_t max_batch_rows;     /* rows packed into one launch */
-  int32_t n_streams;          /* launches in flight */
-  int32_t max_wait_us;        /* how long a batch waits to fill */
-  int32_t reserved;
+  int32_t max_batch_rows;     /* rows packed into one large-lane launch (slice size) */
+  int32_t n_streams;          /* launches in flight per lane */
+  int32_t max_wait_us;        /* how long an idle small-lane batch waits to fill */
+  int32_t small_rows;         /* requests up to this many rows take the small lane; 0 = 4096 */
 } dml_server_config;
 
 typedef struct {

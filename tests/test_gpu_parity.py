@@ -252,3 +252,13 @@ def test_tree_offset_parts_equal_the_whole_forest(dml, algo):
         _assert_same_model(m, nodes, probs, f"part at {t0}")
         acc += f.predict(X)
     assert np.array_equal(acc, whole)
+
+
+@pytest.mark.parametrize("name", ["rf_cls", "rf_reg"])
+def test_plain_predict_matches_predict(dml, name):
+    """The reference-structured predict (one thread per (tree, row), 65,536 per
+    launch) gives dml_predict's votes and sums bit for bit."""
+    gen, kw = CASES[name]
+    X, y = gen()
+    f = dml.fit(X, y, **kw)
+    assert np.array_equal(f.predict_plain(X), f.predict(X))
