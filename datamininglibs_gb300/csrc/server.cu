@@ -12,9 +12,11 @@
 //    thread per row walks every tree).
 // Blocks of a low-priority launch are short (one tile), so a small batch waits
 // for at most one block per SM.  Requests that arrive while batches run join
-// the next batch of their lane as soon as a slot and budget free up.  Pinned
-// host buffers are copied by DMA; pageable ones are staged through pinned
-// slot buffers.  A request completes when all of its rows are back.
+// the next batch of their lane as soon as a slot and budget free up.  A small
+// request whose input and output are both pinned is read and written by the
+// kernel in place through mapped pointers (no copies); other pinned buffers
+// are copied by DMA, pageable ones are staged through pinned slot buffers.  A
+// request completes when all of its rows are back.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -42,14 +44,16 @@ constexpr int kTileRows = 128;      // large lane: rows per tile (one thread per
 constexpr int kSplit = 8;           // small lane: threads per row
 constexpr int kSplitRows = kTileRows / kSplit;
 constexpr int kSplitMaxTrees = 512;  // small-lane regression keeps [rows][trees] leaf values
+constexpr int kSplitMaxFeatures = 1024;  // small-lane tiles stage [features][16 rows] in shared memory
+constexpr int kSplitSmem = 96 * 1024;
 
 struct PredTile {
   const PNode* nodes;
   const float* X;   // feature-major rows of the slice: X[f * n + i]
   float* out;       // [n * width]
-  long long n;      // rows of the slice
+  long long n;      // row pitch of X (rows of the slice or request)
   int row0, rows;   // this tile
-  int n_trees, C, task, pad;
+  int n_trees, C, task, F;
 };
 
 // Large lane: a thread walks every tree for its row (tree order, so regression
@@ -84,31 +88,39 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles(const PredTile* __r
   }
 }
 
-// Small lane: 8 threads per row, thread g walks trees g, g+8, ...; votes meet
-// in shared memory (integer counts, order-free); regression leaf values are
-// kept per tree and summed in tree order by one thread.
+// Small lane: the tile's 16 rows are staged in shared memory (from device
+// staging or straight from the caller's pinned buffer), then 8 threads per row
+// walk trees g, g+8, ...; votes meet in shared memory (integer counts,
+// order-free); regression leaf values are kept per tree and summed in tree
+// order by one thread.
 __global__ void __launch_bounds__(kTileRows) k_predict_tiles_split(
     const PredTile* __restrict__ tiles) {
-  extern __shared__ int sm[];  // votes [kSplitRows][C] or values [kSplitRows][n_trees]
+  extern __shared__ int sm[];  // xs [F][kSplitRows], then votes [kSplitRows][C] or values
   const PredTile t = tiles[blockIdx.x];
   const int g = threadIdx.x % kSplit;
   const int r = threadIdx.x / kSplit;
   const bool act = r < t.rows;
   const long long row = (long long)t.row0 + r;
+  float* xs = reinterpret_cast<float*>(sm);
+  int* acc = sm + t.F * kSplitRows;
+  for (int e = threadIdx.x; e < t.F * kSplitRows; e += kTileRows) {
+    const int f = e / kSplitRows, rr = e % kSplitRows;
+    xs[e] = rr < t.rows ? t.X[(long long)f * t.n + t.row0 + rr] : 0.0f;
+  }
   if (t.task == 0)
-    for (int i = threadIdx.x; i < kSplitRows * t.C; i += kTileRows) sm[i] = 0;
+    for (int i = threadIdx.x; i < kSplitRows * t.C; i += kTileRows) acc[i] = 0;
   __syncthreads();
-  float* vals = reinterpret_cast<float*>(sm) + r * t.n_trees;
+  float* vals = reinterpret_cast<float*>(acc) + r * t.n_trees;
   if (act) {
     for (int k = g; k < t.n_trees; k += kSplit) {
       int4 p = __ldg(reinterpret_cast<const int4*>(t.nodes) + k);
       while (p.x >= 0) {
-        const float x = __ldg(t.X + (long long)p.y * t.n + row);
+        const float x = xs[p.y * kSplitRows + r];
         const int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
         p = __ldg(reinterpret_cast<const int4*>(t.nodes) + nx);
       }
       if (t.task == 0)
-        atomicAdd(&sm[r * t.C + p.y], 1);
+        atomicAdd(&acc[r * t.C + p.y], 1);
       else
         vals[k] = __int_as_float(p.z);
     }
@@ -116,11 +128,11 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles_split(
   __syncthreads();
   if (act) {
     if (t.task == 0) {
-      for (int c = g; c < t.C; c += kSplit) t.out[row * t.C + c] = (float)sm[r * t.C + c];
+      for (int c = g; c < t.C; c += kSplit) t.out[row * t.C + c] = (float)acc[r * t.C + c];
     } else if (g == 0) {
-      float acc = 0.0f;
-      for (int k = 0; k < t.n_trees; ++k) acc = __fadd_rn(acc, vals[k]);
-      t.out[row] = acc;
+      float sum = 0.0f;
+      for (int k = 0; k < t.n_trees; ++k) sum = __fadd_rn(sum, vals[k]);
+      t.out[row] = sum;
     }
   }
 }
@@ -136,6 +148,9 @@ struct Request {
   Clock::time_point t_submit;
   int width, n_features;
   bool pinned_in, pinned_out;
+  bool mapped = false;                 // the small-lane kernel reads and writes the caller's
+  const float* d_samples = nullptr;    // pinned buffers through these device pointers
+  float* d_out = nullptr;
   long long next_row = 0;   // first row not yet handed to a batch
   long long rows_left = 0;  // rows not yet completed
 };
@@ -202,7 +217,8 @@ bool is_pinned(const void* p) {
 }
 
 bool split_ok(const dml_forest* f) {
-  return f->task == DML_CLASSIFICATION || f->n_trees <= kSplitMaxTrees;
+  return f->n_features <= kSplitMaxFeatures &&
+         (f->task == DML_CLASSIFICATION || f->n_trees <= kSplitMaxTrees);
 }
 
 // Completes finished batches; returns true if any slot finished.
@@ -213,7 +229,7 @@ bool reap(dml_server* s) {
     if (cudaEventQuery(sl.batch.done) != cudaSuccess) continue;
     for (const Piece& p : sl.batch.pieces) {
       const Request& r = *p.req;
-      if (!r.pinned_out)
+      if (!r.pinned_out && !(sl.small && r.mapped))
         std::memcpy(r.out + p.row0 * r.width, sl.h_out + p.out_off,
                     sizeof(float) * p.rows * r.width);
     }
@@ -265,11 +281,16 @@ bool launch_batch(dml_server* s, Slot& sl) {
       room = std::min(room, (long long)(sl.cap - out_used) / row_out - 64);
       room = std::min(room, (long long)(sl.tile_cap - tiles) * tile_rows);
       const long long want = r->n - r->next_row;
+      const bool direct = sl.small && r->mapped;  // no staging room needed
+      if (direct)
+        room = std::min(max_rows - rows, (long long)(sl.tile_cap - tiles) * tile_rows);
       if (room <= 0 || (sl.small && room < want)) break;  // small requests are not split
       const long long take = std::min(want, room);
       Piece p{r, r->next_row, take, in_used, out_used};
-      in_used += align256(row_in * take);
-      out_used += align256(row_out * take);
+      if (!direct) {
+        in_used += align256(row_in * take);
+        out_used += align256(row_out * take);
+      }
       rows += take;
       tiles += (int)((take + tile_rows - 1) / tile_rows);
       r->next_row += take;
@@ -284,13 +305,17 @@ bool launch_batch(dml_server* s, Slot& sl) {
   for (const Piece& p : b.pieces) {
     const Request& r = *p.req;
     const dml_forest* f = s->forests[r.forest];
-    char* d_x = sl.d_in + p.in_off;
+    const bool direct = sl.small && r.mapped;
+    char* d_stage = sl.d_in + p.in_off;
+    const float* d_x = direct ? r.d_samples : (const float*)d_stage;
     const size_t rb = sizeof(float) * p.rows;
-    if (r.pinned_in) {
+    if (direct) {
+      // the kernel reads the caller's buffer
+    } else if (r.pinned_in) {
       if (p.rows == r.n)
-        cudaMemcpyAsync(d_x, r.samples, rb * r.n_features, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(d_stage, r.samples, rb * r.n_features, cudaMemcpyHostToDevice, st);
       else
-        cudaMemcpy2DAsync(d_x, rb, r.samples + p.row0, sizeof(float) * r.n, rb, r.n_features,
+        cudaMemcpy2DAsync(d_stage, rb, r.samples + p.row0, sizeof(float) * r.n, rb, r.n_features,
                           cudaMemcpyHostToDevice, st);
     } else {
       char* h = sl.h_in + p.in_off;
@@ -299,24 +324,26 @@ bool launch_batch(dml_server* s, Slot& sl) {
       else
         for (int j = 0; j < r.n_features; ++j)
           std::memcpy(h + rb * j, r.samples + (long long)j * r.n + p.row0, rb);
-      cudaMemcpyAsync(d_x, h, rb * r.n_features, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(d_stage, h, rb * r.n_features, cudaMemcpyHostToDevice, st);
     }
     for (long long r0 = 0; r0 < p.rows; r0 += tile_rows) {
       PredTile& t = sl.h_tiles[nt++];
       t.nodes = f->pnodes;
-      t.X = (const float*)d_x;
-      t.out = (float*)(sl.d_out + p.out_off);
-      t.n = p.rows;
+      t.X = d_x;
+      t.out = direct ? r.d_out : (float*)(sl.d_out + p.out_off);
+      t.n = direct ? r.n : p.rows;
       t.row0 = (int)r0;
       t.rows = (int)std::min<long long>(tile_rows, p.rows - r0);
       t.n_trees = f->n_trees;
       t.C = r.width;
       t.task = f->task;
-      t.pad = 0;
+      t.F = f->n_features;
     }
-    const int need = sl.small ? (f->task == DML_CLASSIFICATION ? kSplitRows * r.width
-                                                               : kSplitRows * f->n_trees)
-                              : (f->task == DML_CLASSIFICATION ? kTileRows * r.width : 1);
+    const int need =
+        sl.small ? kSplitRows * f->n_features + (f->task == DML_CLASSIFICATION
+                                                     ? kSplitRows * r.width
+                                                     : kSplitRows * f->n_trees)
+                 : (f->task == DML_CLASSIFICATION ? kTileRows * r.width : 1);
     shm = std::max(shm, (int)sizeof(int) * need);
   }
   cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, sizeof(PredTile) * nt, cudaMemcpyHostToDevice, st);
@@ -327,6 +354,7 @@ bool launch_batch(dml_server* s, Slot& sl) {
   for (const Piece& p : b.pieces) {
     const Request& r = *p.req;
     const size_t ob = sizeof(float) * p.rows * r.width;
+    if (sl.small && r.mapped) continue;  // written by the kernel
     if (r.pinned_out)
       cudaMemcpyAsync(r.out + p.row0 * r.width, sl.d_out + p.out_off, ob, cudaMemcpyDeviceToHost,
                       st);
@@ -406,6 +434,8 @@ dml_status dml_server_create(const dml_server_config* cfg, dml_server** out) {
   cudaGetDevice(&s->device);
   int prio_low = 0, prio_high = 0;
   cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  cudaFuncSetAttribute(k_predict_tiles_split, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kSplitSmem);
   // a quarter of the budget for the small lane, the rest for the large lane;
   // each slot's share is split between inputs and outputs
   const int ns = cfg->n_streams;
@@ -463,6 +493,18 @@ dml_status dml_server_submit(dml_server* s, int32_t forest_id, const float* samp
   }
   auto r = std::make_shared<Request>();
   const bool pin_in = is_pinned(samples), pin_out = is_pinned(out);
+  if (pin_in && pin_out) {
+    void* dx = nullptr;
+    void* dy = nullptr;
+    if (cudaHostGetDevicePointer(&dx, (void*)samples, 0) == cudaSuccess &&
+        cudaHostGetDevicePointer(&dy, (void*)out, 0) == cudaSuccess) {
+      r->mapped = true;
+      r->d_samples = (const float*)dx;
+      r->d_out = (float*)dy;
+    } else {
+      cudaGetLastError();
+    }
+  }
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (forest_id < 0 || forest_id >= (int32_t)s->forests.size()) {
