@@ -40,7 +40,7 @@ __device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c
   return U4{c0, c1, c2, c3};
 }
 
-enum : uint32_t { kTagFeature = 1, kTagSample = 2, kTagBoot = 3 };
+enum : uint32_t { kTagFeature = 1, kTagSample = 2, kTagBoot = 3, kTagBalanced = 4, kTagPermute = 5 };
 
 // Draw keys: counter = {a, b, tree, tag<<24 | depth}, key = seed.
 __device__ __forceinline__ U4 keyed(uint64_t seed, uint32_t tag, uint32_t depth,

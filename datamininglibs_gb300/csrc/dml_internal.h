@@ -21,6 +21,10 @@ struct ProbDesc {
   int tree0;               // global index of tree 0 of this forest in the batch
   long long ent0;          // entry slot of tree 0; tree t owns [ent0 + t*N, +N)
   int tree_key0;           // RNG tree key of tree 0 (trees sharded across calls)
+  int balanced;            // RF classification: per-class bootstrap (easy ensemble)
+  long long bal_m;         // draws per class: N / C
+  const int* class_rows;   // rows of class c at [class_off[c], class_off[c+1]), ascending
+  const long long* class_off;
 };
 
 // An open node of the current level.  Levels are stored forest-major,

@@ -249,6 +249,11 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       set_error("forest %d: max_depth, min_node_size, n_features_try must be >= 0", i);
       throw InvalidArg{};
     }
+    if (d.balanced != 0 && (d.balanced != 1 || d.algo != DML_ALGO_RF ||
+                            d.task != DML_CLASSIFICATION)) {
+      set_error("forest %d: balanced sampling is for RF classification only", i);
+      throw InvalidArg{};
+    }
     ProbDesc& P = hp[i];
     std::memset(&P, 0, sizeof(P));
     P.N = d.n_rows;
@@ -386,6 +391,20 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       k_prep_targets<<<grid, 256, 0, s>>>(ph[i].y, P.N, P.task, P.S, ph[i].lab, ph[i].q);
       DML_CK(cudaGetLastError());
       ++st.launches;
+      if (descs[i].balanced) {  // per-class row lists for the balanced bootstrap
+        long long* off = (long long*)alloc(sizeof(long long) * (P.C + 1));
+        int* rows = (int*)alloc(sizeof(int) * P.N);
+        DML_CK(cudaMemsetAsync(off, 0, sizeof(long long) * (P.C + 1), s));
+        k_class_count<<<grid, 256, 0, s>>>(ph[i].y, P.N, off);
+        k_class_offsets<<<1, 32, 0, s>>>(off, P.C);
+        k_class_rows<<<P.C, 1024, 0, s>>>(ph[i].y, P.N, off, rows);
+        DML_CK(cudaGetLastError());
+        st.launches += 3;
+        P.balanced = 1;
+        P.bal_m = P.N / P.C;
+        P.class_rows = rows;
+        P.class_off = off;
+      }
     }
     const float2* H = H_n > 0 ? nlogn_table(H_n, s) : nullptr;
 
@@ -898,6 +917,10 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
       d.min_node_size < 0 || d.n_features_try < 0 ||
       (d.task == DML_CLASSIFICATION && d.n_classes < 1)) {
     set_error("invalid fit parameters");
+    return DML_ERR_INVALID_ARG;
+  }
+  if (d.balanced != 0) {
+    set_error("the allocation-free fit has no balanced sampling");
     return DML_ERR_INVALID_ARG;
   }
   if (d.n_rows > kNaMaxRows || (long long)d.n_trees * d.n_rows > kNaMaxSlots ||

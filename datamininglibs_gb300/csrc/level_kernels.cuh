@@ -1,5 +1,6 @@
 // Tiny-node warp kernel, root construction, level scans and model emission.
 #pragma once
+#include "bag.cuh"
 #include "fit_kernels.cuh"
 #include "warp_rf.cuh"
 
@@ -275,7 +276,7 @@ __device__ __forceinline__ bool preleaf(const ProbDesc& P, int n, int depth) {
 #ifndef DML_SEARCH_CW  // driver-only kernels (fit.cu)
 // ============================================================ roots
 // RF bootstrap multiplicities: row r of tree t is drawn w[r] times among the
-// N draws keyed (seed, tree, i) (gpurf.cu:101-113 with keyed draws).
+// tree's bag draws (bag.cuh).
 __global__ void k_boot_count(const ProbDesc* probs, const int* tree_prob, int* wcnt,
                              int chunk) {
   const int gt = blockIdx.y;
@@ -284,12 +285,10 @@ __global__ void k_boot_count(const ProbDesc* probs, const int* tree_prob, int* w
   const int t = gt - P.tree0;
   long long slot0 = P.ent0 + (long long)t * P.N;
   long long beg = (long long)blockIdx.x * chunk;
-  long long end = min(P.N, beg + chunk);
+  long long end = min(bag_draws(P), beg + chunk);
   for (long long i = beg + threadIdx.x; i < end; i += blockDim.x) {
-    U4 r = keyed(P.seed, kTagBoot, 0, (uint32_t)(t + P.tree_key0), (uint32_t)(i >> 2),
-                 (uint32_t)(i >> 34));
-    uint32_t row = pick(r, (int)(i & 3)) % (uint32_t)P.N;
-    atomicAdd(&wcnt[slot0 + row], 1);
+    const long long row = bag_draw(P, t, i);
+    if (row >= 0) atomicAdd(&wcnt[slot0 + row], 1);
   }
 }
 

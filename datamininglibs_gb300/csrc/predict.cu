@@ -9,6 +9,7 @@
 // writes its row once.  Tree order is fixed, so regression sums are
 // deterministic.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -298,6 +299,108 @@ dml_status dml_forest_import(int32_t task, int32_t n_trees, int32_t n_classes, i
   }
   *out = f;
   return DML_OK;
+}
+
+namespace {
+constexpr char kMagic[4] = {'D', 'M', 'L', 'F'};
+constexpr uint32_t kVersion = 1;
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = (const unsigned char*)p;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+}  // namespace
+
+dml_status dml_forest_save(const dml_forest* f, const char* path) {
+  clear_error();
+  if (!f || !path) {
+    set_error("null argument");
+    return DML_ERR_INVALID_ARG;
+  }
+  std::vector<ClassifyNode> nodes((size_t)f->n_nodes);
+  std::vector<float> probs((size_t)f->n_probs);
+  dml_status st = dml_forest_export(f, nodes.data(), probs.data());
+  if (st != DML_OK) return st;
+  const int32_t hdr[4] = {f->task, f->n_trees, f->n_classes, f->n_features};
+  const int64_t sizes[2] = {f->n_nodes, f->n_probs};
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) {
+    set_error("cannot open %s for writing", path);
+    return DML_ERR_INVALID_ARG;
+  }
+  uint64_t h = 14695981039346656037ull;
+  auto put = [&](const void* p, size_t n) {
+    h = fnv1a(h, p, n);
+    return std::fwrite(p, 1, n, fp) == n;
+  };
+  bool ok = put(kMagic, 4) && put(&kVersion, 4) && put(hdr, sizeof(hdr)) &&
+            put(sizes, sizeof(sizes)) && put(nodes.data(), sizeof(ClassifyNode) * nodes.size()) &&
+            put(probs.data(), sizeof(float) * probs.size());
+  ok = ok && std::fwrite(&h, 1, 8, fp) == 8;
+  ok = (std::fclose(fp) == 0) && ok;
+  if (!ok) {
+    set_error("write to %s failed", path);
+    return DML_ERR_INVALID_ARG;
+  }
+  return DML_OK;
+}
+
+dml_status dml_forest_load(const char* path, dml_forest** out) {
+  clear_error();
+  if (!path || !out) {
+    set_error("null argument");
+    return DML_ERR_INVALID_ARG;
+  }
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) {
+    set_error("cannot open %s", path);
+    return DML_ERR_INVALID_ARG;
+  }
+  uint64_t h = 14695981039346656037ull;
+  auto get = [&](void* p, size_t n) {
+    if (std::fread(p, 1, n, fp) != n) return false;
+    h = fnv1a(h, p, n);
+    return true;
+  };
+  char magic[4];
+  uint32_t version = 0;
+  int32_t hdr[4];
+  int64_t sizes[2];
+  std::vector<ClassifyNode> nodes;
+  std::vector<float> probs;
+  bool ok = get(magic, 4) && std::memcmp(magic, kMagic, 4) == 0 && get(&version, 4) &&
+            version == kVersion && get(hdr, sizeof(hdr)) && get(sizes, sizeof(sizes));
+  // sizes must be plausible before allocating: at least a root per tree, and
+  // no more records than the file holds
+  if (ok) {
+    std::fseek(fp, 0, SEEK_END);
+    const long long file_bytes = std::ftell(fp);
+    std::fseek(fp, 4 + 4 + sizeof(hdr) + sizeof(sizes), SEEK_SET);
+    ok = sizes[0] >= 1 && sizes[1] >= 0 &&
+         sizes[0] <= file_bytes / (long long)sizeof(ClassifyNode) &&
+         sizes[1] <= file_bytes / 4 &&
+         (long long)sizeof(ClassifyNode) * sizes[0] + 4 * sizes[1] + 8 + 40 == file_bytes;
+  }
+  if (ok) {
+    nodes.resize((size_t)sizes[0]);
+    probs.resize((size_t)sizes[1]);
+    ok = get(nodes.data(), sizeof(ClassifyNode) * nodes.size()) &&
+         get(probs.data(), sizeof(float) * probs.size());
+  }
+  uint64_t stored = 0;
+  const uint64_t computed = h;
+  ok = ok && std::fread(&stored, 1, 8, fp) == 8 && stored == computed;
+  std::fclose(fp);
+  if (!ok) {
+    set_error("%s is not a valid forest file", path);
+    return DML_ERR_INVALID_ARG;
+  }
+  return dml_forest_import(hdr[0], hdr[1], hdr[2], hdr[3], nodes.data(), sizes[0], probs.data(),
+                           sizes[1], out);
 }
 
 dml_status dml_device_count(int32_t* count) {

@@ -41,7 +41,13 @@ class FitDesc(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("n_rows", ctypes.c_int64),
                 ("n_features", ctypes.c_int32), ("memory", ctypes.c_int32),
                 ("samples", ctypes.c_void_p), ("targets", ctypes.c_void_p),
-                ("tree_offset", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("tree_offset", ctypes.c_int32), ("balanced", ctypes.c_int32)]
+
+
+class OobStats(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_int64), ("pairs_correct", ctypes.c_int64),
+                ("pairs_sq_err", ctypes.c_double), ("rows", ctypes.c_int64),
+                ("rows_correct", ctypes.c_int64), ("rows_sq_err", ctypes.c_double)]
 
 
 class ForestInfo(ctypes.Structure):
@@ -84,6 +90,8 @@ _SIGS = {
     "dml_fit_plain": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_void_p]),
     "dml_last_fit_stats": (ctypes.c_int, [ctypes.POINTER(FitStats)]),
+    "dml_oob_estimate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FitDesc), ctypes.c_int32,
+                                        ctypes.POINTER(OobStats), ctypes.c_void_p]),
     "dml_fit_noalloc": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.c_void_p, ctypes.c_int64,
                                        ctypes.c_void_p, ctypes.c_int64,
                                        ctypes.POINTER(ctypes.c_int64),
@@ -99,6 +107,8 @@ _SIGS = {
                                          ctypes.c_void_p, ctypes.c_int64,
                                          ctypes.POINTER(ctypes.c_void_p)]),
     "dml_forest_free": (None, [ctypes.c_void_p]),
+    "dml_forest_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "dml_forest_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
     "dml_device_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
     "dml_set_device": (ctypes.c_int, [ctypes.c_int32]),
     "dml_last_error": (ctypes.c_char_p, []),
@@ -207,6 +217,17 @@ class Forest:
         _check(fn(self._h, xp, n, op, mem, _stream(stream)))
         return out
 
+    def save(self, path):
+        """dml_forest_save: the forest as a file (reference node layout + hash)."""
+        _check(lib().dml_forest_save(self._h, os.fsencode(path)))
+
+    @staticmethod
+    def load(path):
+        """dml_forest_load: a device-resident forest from a dml_forest_save file."""
+        h = ctypes.c_void_p()
+        _check(lib().dml_forest_load(os.fsencode(path), ctypes.byref(h)))
+        return Forest(h.value)
+
     def free(self):
         if self._h and self._h.value:
             lib().dml_forest_free(self._h)
@@ -230,7 +251,7 @@ class Forest:
 
 
 def _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed,
-          tree_offset=0):
+          tree_offset=0, balanced=0):
     xp, mem = _ptr(X)
     yp, ymem = _ptr(y)
     if mem != ymem:
@@ -238,14 +259,16 @@ def _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_cl
     F, N = X.shape
     return FitDesc(algo, task, n_trees, K, max_depth, min_node_size, min_leaf,
                    n_classes if task == CLASSIFICATION else 1, seed, N, F, mem, xp, yp,
-                   tree_offset, 0)
+                   tree_offset, balanced)
 
 
 def fit(X, y, *, algo, task=CLASSIFICATION, n_trees=100, K=0, max_depth=1000,
-        min_node_size=5, min_leaf=1, n_classes=2, seed=0, tree_offset=0, stream=None):
-    """Defaults are the reference's param pack (ensembles_interface.cc:28-58)."""
+        min_node_size=5, min_leaf=1, n_classes=2, seed=0, tree_offset=0, balanced=0,
+        stream=None):
+    """Defaults are the reference's param pack (ensembles_interface.cc:28-58);
+    balanced=1 is kEasyEnsemble (RF classification)."""
     d = _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed,
-              tree_offset)
+              tree_offset, balanced)
     h = ctypes.c_void_p()
     _check(lib().dml_fit(ctypes.byref(d), ctypes.byref(h), _stream(stream)))
     return Forest(h.value)
@@ -287,6 +310,36 @@ def fit_batched(problems, stream=None):
     out = (ctypes.c_void_p * len(problems))()
     _check(lib().dml_fit_batched(len(problems), descs, out, _stream(stream)))
     return [Forest(out[i]) for i in range(len(problems))]
+
+
+def oob_estimate(forest, X, y, *, seed=0, tree_offset=0, balanced=0, permuted_feature=-1,
+                 stream=None):
+    """dml_oob_estimate: out-of-bag sums of an RF forest fitted on (X, y) with
+    this seed (the bags are drawn again); with permuted_feature >= 0 the
+    permutation run of that feature."""
+    i = forest.info()
+    d = _desc(X, y, ALGO_RF, i.task, i.n_trees, 0, 0, 0, 1, i.n_classes, seed, tree_offset,
+              balanced)
+    st = OobStats()
+    _check(lib().dml_oob_estimate(forest.handle, ctypes.byref(d), permuted_feature,
+                                  ctypes.byref(st), _stream(stream)))
+    return st
+
+
+def feature_importance(forest, X, y, features=None, **kw):
+    """Permutation importance per feature: the drop in out-of-bag pair
+    accuracy (classification) or the rise in out-of-bag pair MSE (regression)
+    when the feature's values come from random rows."""
+    base = oob_estimate(forest, X, y, **kw)
+    feats = range(X.shape[0]) if features is None else features
+    out = []
+    for f in feats:
+        p = oob_estimate(forest, X, y, permuted_feature=int(f), **kw)
+        if forest.info().task == CLASSIFICATION:
+            out.append((base.pairs_correct - p.pairs_correct) / max(1, base.pairs))
+        else:
+            out.append((p.pairs_sq_err - base.pairs_sq_err) / max(1, base.pairs))
+    return np.array(out)
 
 
 def last_fit_stats():

@@ -323,6 +323,11 @@ class DteAlgorithm : public MlAlgorithm<T> {
     d.samples = xs.data();
     d.targets = ys.data();
     d.tree_offset = get_int(params, EnsemblesLib::kTreeOffset, 0);
+    // kEasyEnsemble is read by the reference's RF bootstrap only (gpurf.cu:63-100,
+    // gpudte_algorithm.cc:582-583); ERT uses every row
+    d.balanced = algo_ == DML_ALGO_RF && type == AlgorithmsLib::kClassification &&
+                 params->Has(EnsemblesLib::kEasyEnsemble) &&
+                 params->Get<bool>(EnsemblesLib::kEasyEnsemble);
     auto h = std::make_shared<DeviceForest>();
     dml_status st = dml_fit(&d, &h->f, nullptr);
     if (st != DML_OK) throw_status(st, "Fit");

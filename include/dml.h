@@ -75,7 +75,10 @@ typedef struct {
   /* RNG key of the first tree: a forest fitted as parts with tree_offset =
    * the trees before each part equals the forest fitted at once. */
   int32_t tree_offset;
-  int32_t reserved;
+  /* kEasyEnsemble (gpudte_algorithm.cc:582-583, gpurf.cu:73-100): RF
+   * classification only; each tree draws n_rows / n_classes rows of every
+   * non-empty class, uniformly with replacement, instead of n_rows rows. */
+  int32_t balanced;
 } dml_fit_desc;
 
 typedef struct dml_forest dml_forest;
@@ -143,6 +146,29 @@ DML_API dml_status dml_fit_noalloc(const dml_fit_desc* desc, void* node_array,
 
 DML_API dml_status dml_last_fit_stats(dml_fit_stats* stats);
 
+/* Out-of-bag estimate of an RF forest (gpurf.cu:290-359, kOobEstimate) and the
+ * permutation run of one feature (gpurf.cu:361-438, kFeatureImp).  desc is the
+ * descriptor the forest was fitted with (data, seed, tree_offset, balanced):
+ * the trees' bags are drawn again from it.  Every (tree, row) pair whose row is
+ * out of the tree's bag walks the tree; with permuted_feature >= 0 the value of
+ * that feature is taken from row (Philox(seed; row, tree, kTagPermute) % n_rows)
+ * at every node that splits on it (the reference draws a random row per node
+ * visit).  Sums are reduced in a fixed order.  Permutation importance of a
+ * feature = (pairs_correct - permuted pairs_correct) / pairs for
+ * classification, (permuted pairs_sq_err - pairs_sq_err) / pairs for
+ * regression. */
+typedef struct {
+  int64_t pairs;         /* (tree, row) pairs with the row out of the tree's bag */
+  int64_t pairs_correct; /* classification: pairs whose tree votes the row's class */
+  double pairs_sq_err;   /* regression: sum over pairs of (target - tree output)^2 */
+  int64_t rows;          /* rows out of the bag of at least one tree */
+  int64_t rows_correct;  /* classification: rows whose out-of-bag vote is their class */
+  double rows_sq_err;    /* regression: sum over rows of (target - mean OOB output)^2 */
+} dml_oob_stats;
+
+DML_API dml_status dml_oob_estimate(const dml_forest* forest, const dml_fit_desc* desc,
+                                    int32_t permuted_feature, dml_oob_stats* out, void* stream);
+
 /* GpuDteAlgorithm<T>::Predict (gpudte_algorithm.cc:270-331).  samples is
  * feature-major [n_features * n_rows]; out receives n_rows * n_classes vote
  * counts (classification) or n_rows sums of tree outputs (regression), as
@@ -171,6 +197,15 @@ DML_API dml_status dml_forest_export(const dml_forest* forest, void* node_array,
 DML_API dml_status dml_forest_import(int32_t task, int32_t n_trees, int32_t n_classes,
                                      int32_t n_features, const void* node_array, int64_t n_nodes,
                                      const float* probs, int64_t n_probs, dml_forest** out);
+
+/* Forest files (no counterpart in the reference, whose models live only in
+ * MlModel slots, ml_model_impl.cc:6-10): little-endian
+ *   "DMLF", u32 version = 1, i32 task, n_trees, n_classes, n_features,
+ *   i64 n_nodes, n_probs, the kNodeArray records (20 bytes each),
+ *   the kProbArray floats, u64 FNV-1a hash of everything before it.
+ * Load checks the header, sizes and hash, then imports as dml_forest_import. */
+DML_API dml_status dml_forest_save(const dml_forest* forest, const char* path);
+DML_API dml_status dml_forest_load(const char* path, dml_forest** out);
 
 DML_API void dml_forest_free(dml_forest* forest);
 

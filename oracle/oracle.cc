@@ -92,7 +92,7 @@ W4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
   return o;
 }
 
-enum : uint32_t { kTagFeature = 1, kTagSample = 2, kTagBoot = 3 };
+enum : uint32_t { kTagFeature = 1, kTagSample = 2, kTagBoot = 3, kTagBalanced = 4, kTagPermute = 5 };
 
 inline W4 keyed(uint64_t seed, uint32_t tag, uint32_t depth, uint32_t tree,
                 uint32_t a, uint32_t b) {
@@ -224,9 +224,45 @@ struct Problem {
   int64_t N;
   int F;
   int tree_offset;  // RNG key of tree 0
+  int balanced;     // RF classification: per-class bootstrap (easy ensemble)
   const float* X;  // feature-major [F*N]
   const float* y;  // [N]
 };
+
+// Rows of each class in ascending order (the balanced bootstrap draws from them).
+std::vector<std::vector<int32_t>> class_rows(const float* y, int64_t N, int C) {
+  std::vector<std::vector<int32_t>> r((size_t)C);
+  for (int64_t i = 0; i < N; ++i) r[(size_t)y[i]].push_back((int32_t)i);
+  return r;
+}
+
+// Bootstrap multiplicities of one tree.  Plain (gpurf.cu:101-113 with keyed
+// draws): draw i in [0, N) picks row (word i&3 of Philox(seed; i>>2, i>>34,
+// tree, kTagBoot)) % N.  Balanced, the reference's easy ensemble
+// (gpurf.cu:73-100): for every class c with rows, N / C draws
+// i = c * (N / C) + j pick rows of c uniformly (kTagBalanced); empty classes
+// draw nothing.
+std::vector<int32_t> bag_counts(const Problem& p, int tree,
+                                const std::vector<std::vector<int32_t>>* rows) {
+  const int64_t N = p.N;
+  std::vector<int32_t> w((size_t)N, 0);
+  const uint32_t key = (uint32_t)(tree + p.tree_offset);
+  if (!p.balanced) {
+    for (int64_t i = 0; i < N; ++i) {
+      W4 r = keyed(p.seed, kTagBoot, 0, key, (uint32_t)(i >> 2), (uint32_t)(i >> 34));
+      w[r.v[i & 3] % (uint32_t)N] += 1;
+    }
+    return w;
+  }
+  const int64_t m = N / p.n_classes;
+  for (int64_t i = 0; i < (int64_t)p.n_classes * m; ++i) {
+    const std::vector<int32_t>& rc = (*rows)[(size_t)(i / m)];
+    if (rc.empty()) continue;
+    W4 r = keyed(p.seed, kTagBalanced, 0, key, (uint32_t)(i >> 2), (uint32_t)(i >> 34));
+    w[rc[r.v[i & 3] % (uint32_t)rc.size()]] += 1;
+  }
+  return w;
+}
 
 struct NodeOut {
   int is_leaf;
@@ -282,6 +318,7 @@ struct Ctx {
   std::vector<int32_t> lab;  // classification labels
   std::vector<int64_t> q;    // regression targets, fixed point 2^-S
   int S;
+  std::vector<std::vector<int32_t>> class_rows;  // balanced bootstrap
 };
 
 double h64(double x) { return x <= 1.0 ? 0.0 : x * std::log(x); }
@@ -565,12 +602,7 @@ void fit_tree(const Ctx& cx, int tree, TreeOut& out, bool par_nodes, int threads
   std::vector<Entry> E, E2;
   // root entries: bootstrap multiplicities (RF) or every row once (ERT)
   if (p.algo == 0) {
-    std::vector<int32_t> w((size_t)N, 0);
-    for (int64_t i = 0; i < N; ++i) {
-      W4 r = keyed(p.seed, kTagBoot, 0, (uint32_t)(tree + p.tree_offset), (uint32_t)(i >> 2),
-                   (uint32_t)(i >> 34));
-      w[r.v[i & 3] % (uint32_t)N] += 1;
-    }
+    std::vector<int32_t> w = bag_counts(p, tree, &cx.class_rows);
     for (int64_t i = 0; i < N; ++i)
       if (w[i] > 0) E.push_back(Entry{(int32_t)i, w[i]});
   } else {
@@ -652,7 +684,7 @@ typedef struct {
   int32_t n_features, threads;
   const float* samples;
   const float* targets;
-  int32_t tree_offset, reserved;
+  int32_t tree_offset, balanced;
 } oracle_desc;
 
 // Philox4x32-10 known-answer access for tests.
@@ -742,8 +774,10 @@ void* oracle_fit(const oracle_desc* d) {
   p.X = d->samples;
   p.y = d->targets;
   p.tree_offset = d->tree_offset;
+  p.balanced = d->balanced;
   Ctx cx;
   cx.p = &p;
+  if (p.balanced) cx.class_rows = class_rows(p.y, p.N, p.n_classes);
   std::vector<FF> H;
   if (p.task == 0) {
     H = build_nlogn_table(p.N);
@@ -906,6 +940,130 @@ void oracle_predict(const int32_t* nodes, const float* probs, int n_trees,
       }
     }
   }
+}
+
+// Fixed-shape sum of v[0..n), the engine's order: block b of 256 threads
+// covers [4096 b, 4096 (b+1)), thread j adds items j, j+256, ... in order, then
+// a halving tree (w = 128 .. 1) over the block; the block sums are summed the
+// same way by one block (thread j adds items j, j+256, ...).
+static double tree256(std::vector<double>& sm) {
+  for (int w = 128; w > 0; w >>= 1)
+    for (int j = 0; j < w; ++j) sm[j] = sm[j] + sm[j + w];
+  return sm[0];
+}
+static double fixed_sum(const double* v, int64_t n) {
+  const int64_t nblk = (n + 4095) / 4096;
+  std::vector<double> part((size_t)nblk), sm(256);
+  for (int64_t b = 0; b < nblk; ++b) {
+    for (int j = 0; j < 256; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 16; ++k) {
+        int64_t i = b * 4096 + j + (int64_t)k * 256;
+        if (i < n) s = s + v[i];
+      }
+      sm[j] = s;
+    }
+    part[b] = tree256(sm);
+  }
+  for (int j = 0; j < 256; ++j) {
+    double s = 0.0;
+    for (int64_t i = j; i < nblk; i += 256) s = s + part[i];
+    sm[j] = s;
+  }
+  return tree256(sm);
+}
+
+// Out-of-bag estimate (gpurf.cu:290-359) and the permutation run of one
+// feature (gpurf.cu:361-438), restated: every (tree, row) pair whose row is
+// out of the tree's bag walks the tree; with perm_feature >= 0, nodes that
+// split on it read row Philox(seed; row, row>>32, tree, kTagPermute | depth =
+// feature).x % N instead.  Per row: pairs, correct pairs (classification) or
+// sum of squared errors in tree order (regression), whether the row has a
+// pair, and whether its out-of-bag vote is right (or the squared error of its
+// mean out-of-bag output).  out[0..3] are the fixed-order sums of the four.
+void oracle_oob(const oracle_desc* d, const int32_t* nodes, const float* probs,
+                int perm_feature, double out[4]) {
+  Problem p;
+  p.algo = 0;
+  p.task = d->task;
+  p.n_trees = d->n_trees;
+  p.n_classes = d->task == 0 ? d->n_classes : 1;
+  p.seed = d->seed;
+  p.N = d->n_rows;
+  p.F = d->n_features;
+  p.X = d->samples;
+  p.y = d->targets;
+  p.tree_offset = d->tree_offset;
+  p.balanced = d->balanced;
+  const int64_t N = p.N;
+  const int C = p.n_classes;
+  std::vector<std::vector<int32_t>> rows;
+  if (p.balanced) rows = class_rows(p.y, N, C);
+  std::vector<std::vector<int32_t>> bags((size_t)p.n_trees);
+  for (int t = 0; t < p.n_trees; ++t) bags[t] = bag_counts(p, t, &rows);
+  std::vector<double> acc((size_t)(4 * N), 0.0);
+  for (int64_t i = 0; i < N; ++i) {
+    int64_t pairs = 0, correct = 0;
+    double se = 0.0, vsum = 0.0;
+    std::vector<int64_t> votes((size_t)C, 0);
+    const float target = p.y[i];
+    for (int t = 0; t < p.n_trees; ++t) {
+      if (bags[t][i] > 0) continue;
+      int64_t prow = i;
+      if (perm_feature >= 0) {
+        W4 r = keyed(p.seed, kTagPermute, (uint32_t)perm_feature,
+                     (uint32_t)(t + p.tree_offset), (uint32_t)i, (uint32_t)(i >> 32));
+        prow = r.v[0] % (uint32_t)N;
+      }
+      const int32_t* nd = nodes + (size_t)t * 5;
+      while (nd[1] > 0) {
+        float thr;
+        std::memcpy(&thr, &nd[4], 4);
+        const int64_t r = nd[3] == perm_feature ? prow : i;
+        const float x = p.X[(int64_t)nd[3] * N + r];
+        nd = nodes + (size_t)(goes_left(x, thr) ? nd[0] : nd[0] + 1) * 5;
+      }
+      const float* pr = probs + nd[2];
+      ++pairs;
+      if (p.task == 0) {
+        int sel = 0;
+        float mx = 0.0f;
+        for (int c = 0; c < C; ++c)
+          if (pr[c] > mx) {
+            mx = pr[c];
+            sel = c;
+          }
+        correct += sel == (int)target;
+        votes[sel] += 1;
+      } else {
+        const double v = (double)pr[0];
+        const double e = (double)target - v;
+        se = se + e * e;
+        vsum = vsum + v;
+      }
+    }
+    acc[i] = (double)pairs;
+    acc[N + i] = p.task == 0 ? (double)correct : se;
+    acc[2 * N + i] = pairs > 0 ? 1.0 : 0.0;
+    double ens = 0.0;
+    if (pairs > 0) {
+      if (p.task == 0) {
+        int sel = 0;
+        int64_t mx = 0;
+        for (int c = 0; c < C; ++c)
+          if (votes[c] > mx) {
+            mx = votes[c];
+            sel = c;
+          }
+        ens = sel == (int)target ? 1.0 : 0.0;
+      } else {
+        const double e = (double)target - vsum / (double)pairs;
+        ens = e * e;
+      }
+    }
+    acc[3 * N + i] = ens;
+  }
+  for (int k = 0; k < 4; ++k) out[k] = fixed_sum(acc.data() + (size_t)k * N, N);
 }
 
 }  // extern "C"

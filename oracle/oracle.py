@@ -22,7 +22,7 @@ class OracleDesc(ctypes.Structure):
         ("seed", ctypes.c_uint64), ("n_rows", ctypes.c_int64),
         ("n_features", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("samples", ctypes.c_void_p), ("targets", ctypes.c_void_p),
-        ("tree_offset", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("tree_offset", ctypes.c_int32), ("balanced", ctypes.c_int32),
     ]
 
 
@@ -60,6 +60,8 @@ def lib():
                                         ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_oob.argtypes = [ctypes.POINTER(OracleDesc), ctypes.c_void_p, ctypes.c_void_p,
+                                 ctypes.c_int, ctypes.c_void_p]
         L.oracle_quant_scale.restype = ctypes.c_int
         L.oracle_quant_scale.argtypes = [ctypes.c_void_p, ctypes.c_int64]
         _LIB = L
@@ -90,14 +92,14 @@ class Model:
 
 
 def fit(X, y, *, algo, task=0, n_trees, K=0, max_depth=1000, min_node_size=5, min_leaf=1,
-        n_classes=2, seed=0, threads=0, tree_offset=0):
+        n_classes=2, seed=0, threads=0, tree_offset=0, balanced=0):
     """X: float32 feature-major [F, N]; y: float32 [N]."""
     X = np.ascontiguousarray(X, dtype=np.float32)
     y = np.ascontiguousarray(y, dtype=np.float32)
     F, N = X.shape
     d = OracleDesc(algo, task, n_trees, K, max_depth, min_node_size, min_leaf,
                    n_classes if task == 0 else 1, seed, N, F, threads,
-                   X.ctypes.data, y.ctypes.data, tree_offset, 0)
+                   X.ctypes.data, y.ctypes.data, tree_offset, balanced)
     L = lib()
     h = L.oracle_fit(ctypes.byref(d))
     nn, npb = ctypes.c_int64(), ctypes.c_int64()
@@ -111,6 +113,22 @@ def fit(X, y, *, algo, task=0, n_trees, K=0, max_depth=1000, min_node_size=5, mi
                            g64.ctypes.data, dep.ctypes.data)
     L.oracle_forest_free(h)
     return Model(nodes, probs, n_trees, n_classes if task == 0 else 1, task, g32, g64, dep)
+
+
+def oob(model, X, y, *, seed=0, tree_offset=0, balanced=0, permuted_feature=-1):
+    """Out-of-bag sums of an RF model fitted on (X, y) with this seed:
+    [pairs, correct pairs | squared error, rows, correct rows | squared error]."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    F, N = X.shape
+    d = OracleDesc(0, model.task, model.n_trees, 0, 0, 0, 1, model.n_classes, seed, N, F, 0,
+                   X.ctypes.data, y.ctypes.data, tree_offset, balanced)
+    nodes = np.ascontiguousarray(model.nodes, dtype=np.int32)
+    probs = np.ascontiguousarray(model.probs, dtype=np.float32)
+    out = np.zeros(4, np.float64)
+    lib().oracle_oob(ctypes.byref(d), nodes.ctypes.data, probs.ctypes.data, permuted_feature,
+                     out.ctypes.data)
+    return out
 
 
 def predict(model, X, threads=0):

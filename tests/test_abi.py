@@ -1,0 +1,86 @@
+"""The C ABI without a GPU: the library loads and exports every entry point
+include/dml.h declares, the ctypes mirror has the C layouts, and the checks
+that run before any device work reject bad input."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+HEADER = os.path.join(ROOT, "include", "dml.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from datamininglibs_gb300 import build, ensembles
+    if not os.path.exists(build.LIB):
+        build.build()
+    return ensembles.lib()
+
+
+def declared():
+    text = open(HEADER).read()
+    return re.findall(r"DML_API\s+[\w\s\*]+?\b(dml_\w+)\s*\(", text)
+
+
+def test_every_declared_entry_point_is_exported(lib):
+    names = declared()
+    assert len(names) >= 20
+    from datamininglibs_gb300 import ensembles
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in ensembles._SIGS, "no ctypes signature for " + n
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    from datamininglibs_gb300 import ensembles as e
+    structs = {"dml_fit_desc": e.FitDesc, "dml_forest_info": e.ForestInfo,
+               "dml_fit_stats": e.FitStats, "dml_oob_stats": e.OobStats,
+               "dml_server_config": e.ServerConfig, "dml_server_stats": e.ServerStats}
+    src = tmp_path / "sizes.c"
+    body = "".join('  printf("%s %%zu\\n", sizeof(%s));\n' % (k, k) for k in structs)
+    src.write_text('#include <stdio.h>\n#include "dml.h"\nint main(void) {\n' + body +
+                   "  return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-std=c99", "-I" + os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    for line in out.split("\n"):
+        if line:
+            name, size = line.split()
+            assert int(size) == ctypes.sizeof(structs[name]), name
+
+
+def test_forest_file_checks_run_before_device_work(lib, tmp_path):
+    """A file that is not a forest, a truncated one and one whose hash does not
+    match are refused on the host with DML_ERR_INVALID_ARG."""
+    h = ctypes.c_void_p()
+    bad = tmp_path / "junk.dmlf"
+    bad.write_bytes(b"not a forest file at all" * 4)
+    assert lib.dml_forest_load(os.fsencode(str(bad)), ctypes.byref(h)) == 1
+    assert b"not a valid forest file" in lib.dml_last_error()
+    hdr = b"DMLF" + np.array([1], np.uint32).tobytes() + np.array([0, 1, 2, 3], np.int32).tobytes()
+    hdr += np.array([1, 2], np.int64).tobytes()
+    node = np.array([-1, 0, 0, -1, 0], np.int32).tobytes()
+    probs = np.array([1.0, 0.0], np.float32).tobytes()
+    trunc = tmp_path / "trunc.dmlf"
+    trunc.write_bytes(hdr + node)
+    assert lib.dml_forest_load(os.fsencode(str(trunc)), ctypes.byref(h)) == 1
+    wrong = tmp_path / "hash.dmlf"
+    wrong.write_bytes(hdr + node + probs + b"\0" * 8)
+    assert lib.dml_forest_load(os.fsencode(str(wrong)), ctypes.byref(h)) == 1
+    missing = tmp_path / "missing.dmlf"
+    assert lib.dml_forest_load(os.fsencode(str(missing)), ctypes.byref(h)) == 1
+
+
+def test_server_config_checked_before_device_work(lib):
+    from datamininglibs_gb300 import ensembles as e
+    h = ctypes.c_void_p()
+    for cfg in (e.ServerConfig(0, 1024, 2, 0, 0), e.ServerConfig(1 << 30, 0, 2, 0, 0),
+                e.ServerConfig(1 << 30, 1024, 0, 0, 0), e.ServerConfig(1 << 30, 1024, 2, -1, 0),
+                e.ServerConfig(1 << 30, 1024, 2, 0, -5)):
+        assert lib.dml_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1

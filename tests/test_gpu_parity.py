@@ -262,3 +262,81 @@ def test_plain_predict_matches_predict(dml, name):
     X, y = gen()
     f = dml.fit(X, y, **kw)
     assert np.array_equal(f.predict_plain(X), f.predict(X))
+
+
+def test_balanced_bootstrap_matches_oracle(dml):
+    """kEasyEnsemble (balanced per-class bootstrap) on imbalanced classes, one
+    class empty: trees and votes bit-exact."""
+    X, y = synth.rf_multiclass(3000, 16, n_classes=5, n_int=3, seed=41)
+    y = np.where(y == 4, 1, y).astype(np.float32)  # class 4 empty
+    y[:2500] = np.where(y[:2500] == 3, 0, y[:2500])  # class 3 rare
+    kw = dict(algo=0, n_trees=10, K=5, max_depth=14, min_node_size=5, n_classes=5, seed=8,
+              balanced=1)
+    m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+    _assert_same_model(m, nodes, probs, "balanced")
+    assert np.array_equal(f.predict(X), oracle.predict(m, X))
+    plain = oracle.fit(X, y, **dict(kw, balanced=0))
+    assert plain.nodes.shape != m.nodes.shape or not np.array_equal(plain.nodes, m.nodes)
+
+
+@pytest.mark.parametrize("task", [0, 1])
+@pytest.mark.parametrize("balanced", [0, 1])
+def test_oob_and_permutation_runs_match_oracle(dml, task, balanced):
+    """dml_oob_estimate equals the oracle's restatement bit for bit (counts and
+    fixed-order double sums), for the plain estimate and permutation runs."""
+    if task == 1 and balanced:
+        pytest.skip("balanced sampling is for classification")
+    if task == 0:
+        X, y = synth.rf_multiclass(5000, 14, n_classes=4, n_int=3, seed=51)
+        kw = dict(algo=0, n_trees=9, K=4, max_depth=12, n_classes=4, seed=6, balanced=balanced)
+    else:
+        X, y = synth.rf_regression(5000, 10, seed=52)
+        kw = dict(algo=0, task=1, n_trees=9, K=4, max_depth=12, min_leaf=3, seed=6)
+    m = oracle.fit(X, y, **kw)
+    f = dml.fit(X, y, **kw)
+    for pf in (-1, 0, 5):
+        o = oracle.oob(m, X, y, seed=6, balanced=balanced, permuted_feature=pf)
+        g = dml.oob_estimate(f, X, y, seed=6, balanced=balanced, permuted_feature=pf)
+        assert (g.pairs, g.rows) == (int(o[0]), int(o[2])), pf
+        if task == 0:
+            assert (g.pairs_correct, g.rows_correct) == (int(o[1]), int(o[3])), pf
+        else:
+            assert (g.pairs_sq_err, g.rows_sq_err) == (o[1], o[3]), pf
+    imp = dml.feature_importance(f, X, y, seed=6, balanced=balanced)
+    assert imp.shape == (X.shape[0],) and np.isfinite(imp).all()
+
+
+def test_oob_rejects_ert_and_mismatched_descriptors(dml):
+    X, y = synth.ert_binary(800, 9, seed=3)
+    f = dml.fit(X, y, algo=1, n_trees=4, K=3, max_depth=6, n_classes=2)
+    with pytest.raises(dml.DmlError):
+        dml.ensembles.lib()  # loaded
+        d = dml.ensembles._desc(X, y, 1, 0, 4, 0, 0, 0, 1, 2, 0)
+        st = dml.OobStats()
+        dml.ensembles._check(dml.lib().dml_oob_estimate(f.handle, d, -1, st, None))
+    g = dml.fit(X, y, algo=0, n_trees=4, K=3, max_depth=6, n_classes=2)
+    with pytest.raises(dml.DmlError):
+        dml.oob_estimate(g, X[:5], y, seed=0)  # feature count differs from the forest's
+    with pytest.raises(dml.DmlError):
+        dml.oob_estimate(g, X, y, permuted_feature=9)
+
+
+def test_forest_file_roundtrip(dml, tmp_path):
+    """dml_forest_save / dml_forest_load keep the reference-layout arrays and
+    the votes bit for bit; a flipped byte is refused."""
+    gen, kw = CASES["rf_cls"]
+    X, y = gen()
+    f = dml.fit(X, y, **kw)
+    path = str(tmp_path / "forest.dmlf")
+    f.save(path)
+    g = dml.Forest.load(path)
+    n1, p1 = f.export()
+    n2, p2 = g.export()
+    assert np.array_equal(n1, n2) and np.array_equal(p1, p2)
+    assert np.array_equal(f.predict(X), g.predict(X))
+    raw = bytearray(open(path, "rb").read())
+    raw[100] ^= 0x40
+    bad = str(tmp_path / "bad.dmlf")
+    open(bad, "wb").write(bytes(raw))
+    with pytest.raises(dml.DmlError):
+        dml.Forest.load(bad)

@@ -133,3 +133,25 @@ def test_live_reference_harness():
     X, y = synth.ert_binary(300, 9, seed=17)
     m = oracle.fit(X, y, algo=0, n_trees=7, K=3, max_depth=6, min_node_size=4, n_classes=2, seed=2)
     assert np.array_equal(oracle.predict(m, X), ref.predict(m.nodes, m.probs, 7, 2, 0, X))
+
+
+def test_oracle_bags_out_of_bag_share_and_balance():
+    """Plain bootstrap leaves about e^-1 of the (tree, row) pairs out of the
+    bag; the balanced bootstrap draws N/C rows per non-empty class, so a rare
+    class's rows are almost always in the bag."""
+    from datamininglibs_gb300 import synth
+    X, y = synth.rf_multiclass(4000, 8, n_classes=3, n_int=2, seed=5)
+    m = oracle.fit(X, y, algo=0, n_trees=12, K=3, max_depth=4, n_classes=3, seed=1)
+    o = oracle.oob(m, X, y, seed=1)
+    assert abs(o[0] / (12 * 4000) - np.exp(-1)) < 0.01
+    y2 = y.copy()
+    rare = np.nonzero(y2 == 2)[0][100:]
+    y2[rare] = 0  # class 2 keeps 100 rows
+    mb = oracle.fit(X, y2, algo=0, n_trees=12, K=3, max_depth=4, n_classes=3, seed=1,
+                    balanced=1)
+    ob = oracle.oob(mb, X, y2, seed=1, balanced=1)
+    # class c (n_c rows) gets N // C draws: a row is out of a bag with
+    # probability (1 - 1/n_c)^(N // C)
+    m_draw = 4000 // 3
+    expect = 12 * sum(n * (1 - 1 / n) ** m_draw for n in np.bincount(y2.astype(int)) if n)
+    assert abs(ob[0] / expect - 1) < 0.03
