@@ -2,7 +2,7 @@
 // sort): one CTA per (node, try) work item on a persistent grid, each with its
 // own global scratch.  The sort is an LSD radix sort (8-bit digits) over tiles
 // of 2048 pairs: each warp loads its 256-pair chunk with eight loads in flight,
-// ranks digits stably with __match_any_sync, and the tile is reordered in
+// ranks digits stably within warps (digit_peers), and the tile is reordered in
 // shared memory so that every digit's run is written to global memory as one
 // contiguous stretch.  The boundary scan gives each thread 8 consecutive
 // sorted elements (one block scan of packed class counts per 2048 elements).
@@ -29,6 +29,12 @@ struct BigSmem {
   unsigned long long scan64[kBigWarps];
   unsigned scan32[kBigWarps];
 };
+
+// The value of a sort key of feature f: a rank (looked up) or an orderable key.
+// Equal to from_orderable of the value's key either way (-0 reads as +0).
+__device__ __forceinline__ float key_value(const ProbDesc& P, int f, uint32_t k) {
+  return P.rank ? __ldg(P.vals + (long long)f * P.N + k) : from_orderable(k);
+}
 
 // One LSD pass of pairs (kin, vin) -> (kout, vout) on byte `shift`.
 // Scratch written earlier in the same kernel is read with plain loads (never
@@ -74,14 +80,17 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
     }
     for (int i = threadIdx.x; i < kBigWarps * 256; i += kBigBlock) (&S.whist[0][0])[i] = 0;
     __syncthreads();
+    unsigned pr[kBigPer];  // each element's equal-digit lanes, reused by the scatter
 #pragma unroll
     for (int r = 0; r < kBigPer; ++r) {
       const int i = wbeg + r * 32 + lane;
       const bool act = i < tn;
       const unsigned mask = __ballot_sync(kFull, act);
+      pr[r] = 0;
       if (act) {
         const unsigned dg = (k[r] >> shift) & 255u;
-        const unsigned peers = __match_any_sync(mask, dg);
+        const unsigned peers = digit_peers(mask, dg);
+        pr[r] = peers;
         if ((peers & lt) == 0) S.whist[warp][dg] += __popc(peers);
       }
       __syncwarp();
@@ -109,7 +118,7 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
       const unsigned mask = __ballot_sync(kFull, act);
       if (act) {
         const unsigned dg = (k[r] >> shift) & 255u;
-        const unsigned peers = __match_any_sync(mask, dg);
+        const unsigned peers = pr[r];
         const unsigned pos = S.whist[warp][dg] + __popc(peers & lt);
         S.tk[pos] = k[r];
         S.tv[pos] = v[r];
@@ -394,7 +403,8 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_big_items(BigArgs b) {
       for (int j = 0; j < kBigPer; ++j) {
         const int i = base + j * kBigBlock + threadIdx.x;
         if (i < m) {
-          k1[i] = orderable(__ldg(xf + rr[j]));
+          k1[i] = P.rank ? __ldg(P.rank + (long long)f * P.N + rr[j])
+                         : orderable(__ldg(xf + rr[j]));
           v1[i] = packed ? ((uint32_t)__ldg(P.lab + rr[j]) << 27) |
                                (uint32_t)(wts ? __ldg(wts + i) : 1)
                          : (uint32_t)i;
@@ -439,8 +449,8 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_big_items(BigArgs b) {
       c.f = f;
       // the values on both sides of the boundary (-0 reads back as +0, which
       // gives the same threshold)
-      const float xa = packed ? from_orderable(k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
-      const float xb = packed ? from_orderable(k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
+      const float xa = packed ? key_value(P, f, k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
+      const float xb = packed ? key_value(P, f, k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
       c.thr = midpoint_threshold(xa, xb);
       c.nl_e = bp;
       c.nl = (int)nl;
@@ -584,7 +594,7 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
       const float* xf = P.X + (long long)f * P.N;
       for (int i = threadIdx.x; i < m; i += kBigBlock) {
         const int row = __ldg(rows + i);
-        k1[i] = orderable(__ldg(xf + row));
+        k1[i] = P.rank ? __ldg(P.rank + (long long)f * P.N + row) : orderable(__ldg(xf + row));
         v1[i] = packed ? ((uint32_t)__ldg(P.lab + row) << 27) | (uint32_t)(wts ? __ldg(wts + i) : 1)
                        : (uint32_t)i;
       }
@@ -618,8 +628,8 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
         c.valid = 1;
         c.gain = g;
         c.f = f;
-        const float xa = packed ? from_orderable(k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
-        const float xb = packed ? from_orderable(k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
+        const float xa = packed ? key_value(P, f, k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
+        const float xb = packed ? key_value(P, f, k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
         c.thr = midpoint_threshold(xa, xb);
         c.nl_e = bp;
         c.nl = (int)nl;

@@ -25,6 +25,8 @@ struct ProbDesc {
   long long bal_m;         // draws per class: N / C
   const int* class_rows;   // rows of class c at [class_off[c], class_off[c+1]), ascending
   const long long* class_off;
+  const uint32_t* rank;    // RF: dense value ranks [F * N] (null: sort raw keys)
+  const float* vals;       // RF: value of each rank [F * N]
 };
 
 // An open node of the current level.  Levels are stored forest-major,

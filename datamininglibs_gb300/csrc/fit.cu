@@ -210,6 +210,9 @@ struct ProbHost {
 
 static void finish_stats(dml_fit_stats& st) { g_last_stats = st; }
 
+bool compute_ranks(const float* X, long long N, int F, uint32_t* rank, float* vals,
+                   cudaStream_t s);
+
 static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bool plain,
                                         cudaStream_t s) {
   init_pool_once();
@@ -404,6 +407,19 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
         P.bal_m = P.N / P.C;
         P.class_rows = rows;
         P.class_off = off;
+      }
+      // RF nodes larger than a warp sort value ranks (ranks.cu); the plain
+      // path sorts raw keys, as the reference does
+      if (P.algo == DML_ALGO_RF && P.N > 256 && !plain) {
+        uint32_t* rank = (uint32_t*)alloc(sizeof(uint32_t) * P.N * P.F);
+        float* vals = (float*)alloc(sizeof(float) * P.N * P.F);
+        if (compute_ranks(P.X, P.N, P.F, rank, vals, s)) {
+          P.rank = rank;
+          P.vals = vals;
+          st.launches += 3;
+        } else {
+          clear_error();
+        }
       }
     }
     const float2* H = H_n > 0 ? nlogn_table(H_n, s) : nullptr;

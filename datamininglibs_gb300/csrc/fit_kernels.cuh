@@ -372,8 +372,22 @@ __global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
 // ============================================================ RF (CTA, sorted)
 // Radix sort (LSD, 8-bit digits) of (key, value) pairs held in shared memory
 // or, for large nodes, in global scratch processed tile by tile.  Stability
-// comes from per-warp contiguous chunks and in-order ranking with
-// __match_any_sync.
+// comes from per-warp contiguous chunks and in-order ranking of equal digits
+// within a warp (digit_peers).
+// Lanes of `mask` whose 8-bit digit equals this lane's (what __match_any_sync
+// returns), from one ballot per digit bit: a lane's peers are the lanes that
+// agree with it on every bit.  Every lane of `mask` must call it.
+__device__ __forceinline__ unsigned digit_peers(unsigned mask, unsigned d) {
+  unsigned peers = mask;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const unsigned bit = (d >> b) & 1u;
+    const unsigned bb = __ballot_sync(mask, bit);
+    peers &= bit ? bb : ~bb;
+  }
+  return peers;
+}
+
 template <int BLOCK>
 struct SortSmem {
   unsigned hist[BLOCK / 32][256];
@@ -418,7 +432,7 @@ __device__ void radix_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* k
     if (act) {
       uint32_t k = kin[i], v = vin[i];
       unsigned d = (k >> shift) & 255u;
-      unsigned peers = __match_any_sync(mask, d);
+      unsigned peers = digit_peers(mask, d);
       unsigned pos = S.hist[warp][d] + __popc(peers & lt);
       kout[pos] = k;
       vout[pos] = v;
