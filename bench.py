@@ -109,13 +109,16 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """DRAM bytes per unit of the search kernels from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "rf_search_kernels_c2.md")
+def traffic_from_profile(kernel):
+    """DRAM bytes per tried entry of a search kernel, measured by ncu on the
+    200k x 64 case (profiles/search_kernels_rf_multiclass.md, lines
+    `dram_bytes_per_entry_try <kernel>: <bytes>`); scaled to a launch by the
+    launch's tried entries."""
+    path = os.path.join(ROOT, "profiles", "search_kernels_rf_multiclass.md")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_entry_try:"):
-                return float(line.split(":")[1])
+            if line.startswith("dram_bytes_per_entry_try " + kernel + ":"):
+                return float(line.split(":")[-1])
     except OSError:
         pass
     return None
@@ -138,19 +141,21 @@ def cpu_baseline(w, X, y, threads, trees):
 
 
 def run_reference(args, w):
-    """The reference path's CPU restatement timed on the host cores; each step
-    builds one tree of the workload with every host thread."""
+    """The reference path's CPU restatement timed on the host cores.  A timed
+    step builds as many of the workload's trees as there are host threads, one
+    tree per thread (the way the CPU is used best); a warm-up step builds one."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     X, y = make_data(w)
     threads = os.cpu_count() or 1
+    trees = min(threads, w["trees"])
     for _ in range(args.warmup):
         cpu_baseline(w, X, y, threads, 1)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(w, X, y, threads, 1))
+        vals.append(cpu_baseline(w, X, y, threads, trees))
     total = time.perf_counter() - t0
     value = float(np.mean([v["value"] for v in vals]))
     cb = dict(vals[-1])
@@ -159,7 +164,9 @@ def run_reference(args, w):
             "unit": "nodes/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * total / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-            "config": {"workload": w["name"], "sample": "one tree per step, all host threads"},
+            "config": {"workload": w["name"],
+                       "sample": "%d of the %d trees per step, one per host thread" % (
+                           trees, w["trees"])},
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "nodes/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -317,6 +324,8 @@ def run_ours(args, w):
     e1 = torch.cuda.Event(enable_timing=True)
     nodes = entries = entry_tries = launches = 0
     search_ms = loop_ms = 0.0
+    nq = dml.ensembles.NUM_QUEUES
+    q_ms, q_ent, q_tries, q_launch = [0.0] * nq, [0] * nq, [0] * nq, [0] * nq
     e0.record(stream)
     for _ in range(args.steps):
         f = dml.fit(Xd, yd, stream=stream, **kw)
@@ -327,6 +336,11 @@ def run_ours(args, w):
         launches += st.launches
         search_ms += st.search_ms
         loop_ms += st.level_loop_ms
+        for q in range(nq):
+            q_ms[q] += st.queue_ms[q]
+            q_ent[q] += st.queue_entries[q]
+            q_tries[q] += st.queue_entry_tries[q]
+            q_launch[q] += st.queue_launches[q]
         last_forest = f
         if _ != args.steps - 1:
             f.free()
@@ -396,9 +410,19 @@ def run_ours(args, w):
             dist.destroy_process_group()
         return
     peak, peak_kind = measured_peak()
-    alg_bytes = 4.0 * entry_tries + 20.0 * entries
-    achieved = alg_bytes / (search_ms / 1000.0) / 1e9 if search_ms > 0 else None
-    tpu = traffic_from_profile()
+    # the dominant kernel: the node class with the most device time; its
+    # algorithmic bytes (4 per tried entry, 20 per searched entry) over its
+    # CUDA-event time on the fit stream
+    names = dml.ensembles.QUEUE_KERNELS
+    dom = max(range(nq), key=lambda q: q_ms[q])
+    alg_q = [4.0 * q_tries[q] + 20.0 * q_ent[q] for q in range(nq)]
+    achieved = alg_q[dom] / (q_ms[dom] / 1000.0) / 1e9 if q_ms[dom] > 0 else None
+    tpu = traffic_from_profile(names[dom])
+    queues = {names[q]: {"ms_per_fit": q_ms[q] / args.steps,
+                         "share": q_ms[q] / search_ms if search_ms > 0 else None,
+                         "launches_per_fit": q_launch[q] / args.steps,
+                         "algorithmic_GBps": alg_q[q] / (q_ms[q] / 1000.0) / 1e9}
+              for q in range(nq) if q_ms[q] > 0}
     line = {
         "metric": "rf_build_nodes_per_s", "value": value, "unit": "nodes/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -416,13 +440,16 @@ def run_ours(args, w):
         "forest": {"nodes": finfo.n_nodes, "max_depth": finfo.max_depth},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "traffic": (tpu * entry_tries / args.steps / max(1, launches))
-                     if tpu else None,
-                     "kernel": "split search (k_group_nodes, k_warp_rf, k_rf_smem, k_rf_big_items, k_ert_cta)",
-                     "algorithmic_bytes_per_fit": alg_bytes / args.steps,
+                     "traffic": (tpu * q_tries[dom] / max(1, q_launch[dom])) if tpu else None,
+                     "kernel": names[dom],
+                     "algorithmic_bytes_per_launch": alg_q[dom] / max(1, q_launch[dom]),
+                     "launches": q_launch[dom],
                      "peak_kind": peak_kind,
                      "search_ms_per_fit": search_ms / args.steps,
-                     "level_loop_ms_per_fit": loop_ms / args.steps},
+                     "level_loop_ms_per_fit": loop_ms / args.steps,
+                     "search_algorithmic_GBps": (4.0 * entry_tries + 20.0 * entries)
+                     / (search_ms / 1000.0) / 1e9 if search_ms > 0 else None},
+        "search_kernels": queues,
         "e2e": {"value": e2e_nodes / e2e_s, "unit": "nodes/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h // e2e_steps},
         "gpu_launches": launches,

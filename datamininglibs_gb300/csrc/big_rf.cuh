@@ -471,7 +471,10 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_big_items(BigArgs b) {
       c.suml = 0;
       *cout = c;
     }
-    if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)m);
+    if (threadIdx.x == 0) {
+      atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)m);
+      if (b.phase == 1 && ts == 0) atomicAdd((unsigned long long*)&a.stats[3], (unsigned long long)m);
+    }
     __syncthreads();
   }
 }
@@ -675,7 +678,10 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
       if (stop) break;
     }
     const Cand b = s_best;
-    if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)t * m);
+    if (threadIdx.x == 0) {
+      atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)t * m);
+      atomicAdd((unsigned long long*)&a.stats[3], (unsigned long long)m);
+    }
     if (!b.valid) {
       if (threadIdx.x == 0) write_leaf(a.res, node);
     } else {

@@ -19,6 +19,13 @@
 #include "level_kernels.cuh"
 #include "search_launch.cuh"
 
+static_assert(dml::kNumQ == DML_NUM_QUEUES && dml::kQWarp == DML_Q_WARP32 &&
+                  dml::kQErt == DML_Q_ERT && dml::kQRfSmall == DML_Q_RF_SMEM &&
+                  dml::kQRfBig == DML_Q_RF_BIG && dml::kQRfW2 == DML_Q_RF_W64 &&
+                  dml::kQRfW4 == DML_Q_RF_W128 && dml::kQRfW8 == DML_Q_RF_W256 &&
+                  dml::kQG16 == DML_Q_GROUP16 && dml::kQG8 == DML_Q_GROUP8,
+              "node classes of the engine and of include/dml.h agree");
+
 namespace dml {
 
 namespace {
@@ -466,8 +473,10 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     }
     int* d_qcount = (int*)alloc(sizeof(int) * kNumQ);
     int* d_summary = (int*)alloc(sizeof(int) * 2);
-    long long* d_stats = (long long*)alloc(sizeof(long long) * 4);
-    DML_CK(cudaMemsetAsync(d_stats, 0, sizeof(long long) * 4, s));
+    // [0..3] fit totals, then 4 per node class: [2] tries x entries, [3] entries
+    constexpr int kStatWords = 4 + 4 * kNumQ;
+    long long* d_stats = (long long*)alloc(sizeof(long long) * kStatWords);
+    DML_CK(cudaMemsetAsync(d_stats, 0, sizeof(long long) * kStatWords, s));
     Summary* h_sum = nullptr;
     DML_CK(cudaMallocHost(&h_sum, sizeof(Summary)));
 
@@ -511,11 +520,15 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     long long log_base = 0, plog_base = 0;
     int depth = 0;
     float search_ms_total = 0.0f;
-    cudaEvent_t es0, es1, tq0, tq1;
+    cudaEvent_t es0, es1, qev[kNumQ][2];
     DML_CK(cudaEventCreate(&es0));
     DML_CK(cudaEventCreate(&es1));
-    DML_CK(cudaEventCreate(&tq0));
-    DML_CK(cudaEventCreate(&tq1));
+    for (auto& e : qev) {
+      DML_CK(cudaEventCreate(&e[0]));
+      DML_CK(cudaEventCreate(&e[1]));
+    }
+    double queue_ms[kNumQ] = {};
+    int queue_launches[kNumQ] = {};
     const char* tenv = getenv("DML_TRACE");
     const bool trace = tenv && tenv[0] == '1';
     while (n > 0) {
@@ -567,7 +580,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           b.nretry_out = d_nretry;
           b.big_index = big_index.p;
           DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
-          if (trace) DML_CK(cudaEventRecord(tq0, s));
+          b.L.stats = d_stats + 4 + 4 * q;
+          DML_CK(cudaEventRecord(qev[q][0], s));
           const int chunk = plain ? kPlainChunk : nb;
           for (int off = 0; off < nb; off += chunk) {
             b.big = qlist[q].p + off;
@@ -576,33 +590,30 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
             launch_big(CW, b, 1, big_grid, std::min(b.nbig, 65535), max_mand, s);
             launch_big(CW, b, 2, big_grid, std::min(b.nbig, 65535), std::max(1, max_opt), s);
             st.launches += 4;
+            queue_launches[q] += 4;
             if (plain) DML_CK(cudaStreamSynchronize(s));
           }
-          if (trace) {
-            DML_CK(cudaEventRecord(tq1, s));
-            DML_CK(cudaEventSynchronize(tq1));
-            cudaEventElapsedTime(&qms[q], tq0, tq1);
-          }
+          DML_CK(cudaEventRecord(qev[q][1], s));
           continue;
         }
+        LevelArgs aq = a;
+        aq.stats = d_stats + 4 + 4 * q;
+        DML_CK(cudaEventRecord(qev[q][0], s));
         if (!plain) {
-          a.work = qlist[q].p;
-          if (trace) DML_CK(cudaEventRecord(tq0, s));
-          launch_search(CW, q, a, qc[q], s);
-          if (trace) {
-            DML_CK(cudaEventRecord(tq1, s));
-            DML_CK(cudaEventSynchronize(tq1));
-            cudaEventElapsedTime(&qms[q], tq0, tq1);
-          }
+          aq.work = qlist[q].p;
+          launch_search(CW, q, aq, qc[q], s);
           ++st.launches;
+          ++queue_launches[q];
         } else {
           for (int off = 0; off < qc[q]; off += kPlainChunk) {
-            a.work = qlist[q].p + off;
-            launch_search(CW, q, a, std::min(kPlainChunk, qc[q] - off), s);
+            aq.work = qlist[q].p + off;
+            launch_search(CW, q, aq, std::min(kPlainChunk, qc[q] - off), s);
             ++st.launches;
+            ++queue_launches[q];
             DML_CK(cudaStreamSynchronize(s));
           }
         }
+        DML_CK(cudaEventRecord(qev[q][1], s));
       }
       DML_CK(cudaEventRecord(es1, s));
       // -------------------------------------------------- scans
@@ -663,6 +674,11 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       DML_CK(cudaStreamSynchronize(s));
       float sm = 0.0f;
       cudaEventElapsedTime(&sm, es0, es1);
+      for (int q = 0; q < kNumQ; ++q)
+        if (qc[q] > 0) {
+          cudaEventElapsedTime(&qms[q], qev[q][0], qev[q][1]);
+          queue_ms[q] += qms[q];
+        }
       search_ms_total += sm;
       if (trace)
         fprintf(stderr,
@@ -672,6 +688,20 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
                 depth, n, qc[kQG8], qms[kQG8], qc[kQG16], qms[kQG16], qc[kQWarp], qms[kQWarp],
                 qc[kQErt], qms[kQErt], qc[kQRfW2], qms[kQRfW2], qc[kQRfW4], qms[kQRfW4], qc[kQRfW8],
                 qms[kQRfW8], qc[kQRfSmall], qms[kQRfSmall], qc[kQRfBig], qms[kQRfBig], sm);
+      if (trace) {  // per class: entries and tries x entries searched at this level
+        static long long prev[kStatWords];
+        long long cur_st[kStatWords];
+        if (depth == 0) std::memset(prev, 0, sizeof(prev));
+        DML_CK(cudaMemcpy(cur_st, d_stats, sizeof(cur_st), cudaMemcpyDeviceToHost));
+        fprintf(stderr, "[dml] level %2d work", depth);
+        for (int q = 0; q < kNumQ; ++q)
+          if (qc[q] > 0)
+            fprintf(stderr, " | q%d entries %lld tries %lld", q,
+                    cur_st[4 + 4 * q + 3] - prev[4 + 4 * q + 3],
+                    cur_st[4 + 4 * q + 2] - prev[4 + 4 * q + 2]);
+        fprintf(stderr, "\n");
+        std::memcpy(prev, cur_st, sizeof(prev));
+      }
       log_base += n;
       plog_base += h_sum->leaves;
       n = h_sum->children;
@@ -690,15 +720,24 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     cudaEventDestroy(ev1);
     cudaEventDestroy(es0);
     cudaEventDestroy(es1);
-    cudaEventDestroy(tq0);
-    cudaEventDestroy(tq1);
-    long long h_stats[4];
+    for (auto& e : qev) {
+      cudaEventDestroy(e[0]);
+      cudaEventDestroy(e[1]);
+    }
+    long long h_stats[kStatWords];
     DML_CK(cudaMemcpy(h_stats, d_stats, sizeof(h_stats), cudaMemcpyDeviceToHost));
     cudaFreeHost(h_sum);
     st.nodes = log_base;
     st.entries = h_stats[0];
     st.weighted_rows = h_stats[1];
-    st.entry_tries = h_stats[2];
+    st.entry_tries = 0;
+    for (int q = 0; q < kNumQ; ++q) {
+      st.queue_ms[q] = queue_ms[q];
+      st.queue_launches[q] = queue_launches[q];
+      st.queue_entry_tries[q] = h_stats[4 + 4 * q + 2];
+      st.queue_entries[q] = h_stats[4 + 4 * q + 3];
+      st.entry_tries += st.queue_entry_tries[q];
+    }
     st.levels = depth;
     st.level_loop_ms = loop_ms;
     st.search_ms = search_ms_total;

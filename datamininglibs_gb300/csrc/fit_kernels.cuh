@@ -184,7 +184,7 @@ struct LevelArgs {
   uint2* scratch;       // two pair buffers per entry slot: scratch[slot], scratch[slot + total]
   long long scratch_half;
   const float2* H;      // n*ln(n) table
-  long long* stats;     // [2] += tries evaluated x node entries
+  long long* stats;     // [2] += tries evaluated x node entries, [3] += node entries
 };
 
 // ================================================================== ERT (CTA)
@@ -354,9 +354,11 @@ __global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
       }
     }
     const Cand b = s_best;
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
       atomicAdd((unsigned long long*)&a.stats[2],
                 (unsigned long long)tries_done * nd.ecnt);
+      atomicAdd((unsigned long long*)&a.stats[3], (unsigned long long)nd.ecnt);
+    }
     if (!b.valid) {
       if (threadIdx.x == 0) write_leaf(a.res, node);
     } else {

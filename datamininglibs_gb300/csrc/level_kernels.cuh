@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(256, 2) k_group_nodes(LevelArgs a) {
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nslots = (a.nwork + NPW - 1) / NPW;
-  unsigned long long tries_done = 0;  // entry-tries evaluated (on group leaders)
+  unsigned long long tries_done = 0, entries_done = 0;  // on group leaders
   for (int ws = gw; ws < nslots; ws += nwarps) {
     const int wi = ws * NPW + gi;
     if (wi >= a.nwork) continue;
@@ -201,7 +201,10 @@ __global__ void __launch_bounds__(256, 2) k_group_nodes(LevelArgs a) {
         more = !(cd.valid && cd.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
       }
       if (!more) {
-        if (gl == 0) tries_done += (unsigned long long)(t + 1) * m;
+        if (gl == 0) {
+          tries_done += (unsigned long long)(t + 1) * m;
+          entries_done += m;
+        }
         break;
       }
     }
@@ -227,7 +230,11 @@ __global__ void __launch_bounds__(256, 2) k_group_nodes(LevelArgs a) {
     }
   }
   tries_done = warp_sum<unsigned long long>(tries_done);
-  if (lane == 0 && tries_done) atomicAdd((unsigned long long*)&a.stats[2], tries_done);
+  entries_done = warp_sum<unsigned long long>(entries_done);
+  if (lane == 0 && tries_done) {
+    atomicAdd((unsigned long long*)&a.stats[2], tries_done);
+    atomicAdd((unsigned long long*)&a.stats[3], entries_done);
+  }
 }
 
 // ============================================================ work queues

@@ -258,7 +258,10 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
       }
       if (!more) break;
     }
-    if (lane == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)(t + 1) * m);
+    if (lane == 0) {
+      atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)(t + 1) * m);
+      atomicAdd((unsigned long long*)&a.stats[3], (unsigned long long)m);
+    }
     if (!best.valid) {
       if (lane == 0) write_leaf(a.res, node);
       __syncwarp();

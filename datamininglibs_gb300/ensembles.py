@@ -58,12 +58,23 @@ class ForestInfo(ctypes.Structure):
                 ("fit_ms", ctypes.c_double)]
 
 
+NUM_QUEUES = 9
+# kernel that searches each node class (DML_Q_* in include/dml.h)
+QUEUE_KERNELS = ["k_group_nodes<32>", "k_ert_cta", "k_rf_smem", "k_rf_big_items+k_rf_big_decide",
+                 "k_warp_rf<2>", "k_warp_rf<4>", "k_warp_rf<8>", "k_group_nodes<16>",
+                 "k_group_nodes<8>"]
+
+
 class FitStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_int64), ("entries", ctypes.c_int64),
                 ("weighted_rows", ctypes.c_int64), ("entry_tries", ctypes.c_int64),
                 ("levels", ctypes.c_int32),
                 ("launches", ctypes.c_int32), ("level_loop_ms", ctypes.c_double),
-                ("search_ms", ctypes.c_double)]
+                ("search_ms", ctypes.c_double),
+                ("queue_ms", ctypes.c_double * NUM_QUEUES),
+                ("queue_entries", ctypes.c_int64 * NUM_QUEUES),
+                ("queue_entry_tries", ctypes.c_int64 * NUM_QUEUES),
+                ("queue_launches", ctypes.c_int32 * NUM_QUEUES), ("reserved", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -95,6 +95,21 @@ typedef struct {
   double fit_ms;     /* device time of the level loop of the fit that built it */
 } dml_forest_info;
 
+/* Node classes of the split search (the index of the per-class statistics)
+ * and the kernels that search them. */
+enum {
+  DML_Q_WARP32 = 0,   /* <= 32 entries, one warp per node (k_group_nodes<32>) */
+  DML_Q_ERT = 1,      /* ERT, > 32 entries, one CTA per node (k_ert_cta) */
+  DML_Q_RF_SMEM = 2,  /* RF, 257..4096 entries, CTA, shared-memory sort (k_rf_smem) */
+  DML_Q_RF_BIG = 3,   /* RF, > 4096 entries, per-try items (k_rf_big_items + _decide) */
+  DML_Q_RF_W64 = 4,   /* RF, 33..64 entries, warp register sort (k_warp_rf<2>) */
+  DML_Q_RF_W128 = 5,  /* RF, 65..128 entries (k_warp_rf<4>) */
+  DML_Q_RF_W256 = 6,  /* RF, 129..256 entries (k_warp_rf<8>) */
+  DML_Q_GROUP16 = 7,  /* <= 16 entries, 16 lanes per node (k_group_nodes<16>) */
+  DML_Q_GROUP8 = 8,   /* <= 8 entries, 8 lanes per node (k_group_nodes<8>) */
+  DML_NUM_QUEUES = 9
+};
+
 /* Fit statistics of the last dml_fit/dml_fit_batched on this thread. */
 typedef struct {
   int64_t nodes;         /* internal + leaf nodes created, all forests */
@@ -105,6 +120,13 @@ typedef struct {
   int32_t launches;      /* kernel launches of the fit */
   double level_loop_ms;  /* device time of the level loop (CUDA events) */
   double search_ms;      /* device time in the split-search kernels */
+  /* per node class (DML_Q_*): device time (CUDA events around the class's
+   * launches on the fit stream), searched entries, tries x entries */
+  double queue_ms[DML_NUM_QUEUES];
+  int64_t queue_entries[DML_NUM_QUEUES];
+  int64_t queue_entry_tries[DML_NUM_QUEUES];
+  int32_t queue_launches[DML_NUM_QUEUES]; /* kernel launches per class */
+  int32_t reserved;
 } dml_fit_stats;
 
 /* GpuDteAlgorithm<T>::Fit (lib_ensembles/source/gpudte_algorithm.cc:15-267),
