@@ -311,42 +311,87 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
       for (int c = 0; c < CW; ++c) runL[c] = 0;
     }
     uint32_t prevk = prevk0;
-#pragma unroll
-    for (int j = 0; j < kBigPer; ++j) {
-      const int p = p0 + j;
-      if (p < m && p > 0 && prevk < kk[j]) {
-        const long long nr = (long long)nd.n - run_n;
-        if (run_n >= ml && nr >= ml) {
-          float g;
-          if (P.task == 0)
-            g = entropy_gain_u<2 * CW>(
+    if (packed) {
+      // classification: a rolled loop that re-reads each (key, label|weight)
+      // pair; the 2C-term entropy gain is the bulk of the kernel's code and
+      // unrolled eight times it overflows the instruction cache
+#pragma unroll 1
+      for (int j = 0; j < kBigPer; ++j) {
+        const int p = p0 + j;
+        uint32_t kj = 0xFFFFFFFFu;
+        int wj = 0, labj = -1;
+        if (p < m) {
+          kj = sk[p];
+          const uint32_t vv = sv[p];
+          labj = (int)(vv >> 27);
+          wj = (int)(vv & 0x7FFFFFFu);
+        }
+        if (p < m && p > 0 && prevk < kj) {
+          const long long nr = (long long)nd.n - run_n;
+          if (run_n >= ml && nr >= ml) {
+            const float g = entropy_gain_u<2 * CW>(
                 H, prior, C, run_n, nr,
                 [&](int c) {
                   return (long long)((c & 1) ? (runL[c >> 1] >> 32)
                                              : (runL[c >> 1] & 0xFFFFFFFFull));
                 },
                 [&](int c) { return (long long)Nt[c]; });
-          else
-            g = variance_gain(run_n, run_s, nr, nd.sum - run_s, P.S);
-          if (bp < 0 || g > bg) {
-            bg = g;
-            bp = p;
-            bnl = run_n;
-            bsl = run_s;
+            if (bp < 0 || g > bg) {
+              bg = g;
+              bp = p;
+              bnl = run_n;
 #pragma unroll
-            for (int c = 0; c < CW; ++c) bL[c] = runL[c];
+              for (int c = 0; c < CW; ++c) bL[c] = runL[c];
+            }
           }
         }
-      }
-      prevk = kk[j];
-      run_n += w[j];
-      if (P.task == 0) {
+        prevk = kj;
+        run_n += wj;
 #pragma unroll
         for (int c = 0; c < CW; ++c)
-          runL[c] += (lab[j] == 2 * c ? (unsigned long long)w[j] : 0ull) |
-                     (lab[j] == 2 * c + 1 ? ((unsigned long long)w[j] << 32) : 0ull);
-      } else {
-        run_s += q[j] * (long long)w[j];
+          runL[c] += (labj == 2 * c ? (unsigned long long)wj : 0ull) |
+                     (labj == 2 * c + 1 ? ((unsigned long long)wj << 32) : 0ull);
+      }
+    } else {
+      // entry-indexed values (regression, or unpacked labels): the gathered
+      // weights and targets stay in registers, all loads already in flight
+#pragma unroll
+      for (int j = 0; j < kBigPer; ++j) {
+        const int p = p0 + j;
+        if (p < m && p > 0 && prevk < kk[j]) {
+          const long long nr = (long long)nd.n - run_n;
+          if (run_n >= ml && nr >= ml) {
+            float g;
+            if (P.task == 0)
+              g = entropy_gain_u<2 * CW>(
+                  H, prior, C, run_n, nr,
+                  [&](int c) {
+                    return (long long)((c & 1) ? (runL[c >> 1] >> 32)
+                                               : (runL[c >> 1] & 0xFFFFFFFFull));
+                  },
+                  [&](int c) { return (long long)Nt[c]; });
+            else
+              g = variance_gain(run_n, run_s, nr, nd.sum - run_s, P.S);
+            if (bp < 0 || g > bg) {
+              bg = g;
+              bp = p;
+              bnl = run_n;
+              bsl = run_s;
+#pragma unroll
+              for (int c = 0; c < CW; ++c) bL[c] = runL[c];
+            }
+          }
+        }
+        prevk = kk[j];
+        run_n += w[j];
+        if (P.task == 0) {
+#pragma unroll
+          for (int c = 0; c < CW; ++c)
+            runL[c] += (lab[j] == 2 * c ? (unsigned long long)w[j] : 0ull) |
+                       (lab[j] == 2 * c + 1 ? ((unsigned long long)w[j] << 32) : 0ull);
+        } else {
+          run_s += q[j] * (long long)w[j];
+        }
       }
     }
   }

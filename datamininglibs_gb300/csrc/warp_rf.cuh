@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
   __shared__ int s_w[WPB][M];
   __shared__ int s_lab[WPB][M];
   __shared__ long long s_q[WPB][M];
+  __shared__ unsigned long long s_key[WPB][M];  // sorted (key, entry) of the current try
   const int lane = threadIdx.x & 31;
   const int wb = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -127,7 +128,11 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
                        : ~0ull;
       }
       warp_bitonic_sort<E>(key);
-      // boundary scan, 32 sorted elements per round
+#pragma unroll
+      for (int r = 0; r < E; ++r) s_key[wb][r * 32 + lane] = key[r];
+      __syncwarp();
+      // boundary scan, 32 sorted elements per round (a rolled loop: the
+      // per-round class scans and gains are the bulk of the kernel's code)
       unsigned long long carryL[CW], L[CW], myL[CW];
 #pragma unroll
       for (int j = 0; j < CW; ++j) {
@@ -138,9 +143,9 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
       uint32_t lastk = 0;
       float bg = -FLT_MAX;
       int bp = -1;
-#pragma unroll
+#pragma unroll 1
       for (int r = 0; r < E; ++r) {
-        const unsigned long long kv = key[r];
+        const unsigned long long kv = s_key[wb][r * 32 + lane];
         const bool ok = kv != ~0ull;
         const int e = (int)(kv & 0xFFFFFFFFull);
         const uint32_t kk = (uint32_t)(kv >> 32);
@@ -215,15 +220,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
         cd.valid = 1;
         cd.gain = wg;
         // entries at sorted positions wp-1 and wp
-        const int ra = (wp - 1) >> 5, la = (wp - 1) & 31, rb = wp >> 5, lb = wp & 31;
-        unsigned long long ka = key[0], kb = key[0];
-#pragma unroll
-        for (int r = 1; r < E; ++r) {
-          if (r == ra) ka = key[r];
-          if (r == rb) kb = key[r];
-        }
-        ka = __shfl_sync(kFull, ka, la);
-        kb = __shfl_sync(kFull, kb, lb);
+        const unsigned long long ka = s_key[wb][wp - 1], kb = s_key[wb][wp];
         const float xa = __ldg(xf + s_row[wb][(int)(ka & 0xFFFFFFFFull)]);
         const float xb = __ldg(xf + s_row[wb][(int)(kb & 0xFFFFFFFFull)]);
         cd.thr = midpoint_threshold(xa, xb);
@@ -256,6 +253,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
 #pragma unroll
         for (int j = 0; j < CW; ++j) bestL[j] = candL[j];
       }
+      __syncwarp();
       if (!more) break;
     }
     if (lane == 0) {
