@@ -19,6 +19,10 @@ constexpr int kBigPer = 8;                       // elements per thread
 constexpr int kBigTile = kBigBlock * kBigPer;    // 2048
 constexpr int kBigWarps = kBigBlock / 32;
 
+// Resident CTAs per SM of the item kernel: three where the class counts are
+// narrow enough to fit 80 registers without spilling much, else two.
+constexpr int big_ctas_per_sm(int cw) { return cw <= 2 ? 3 : 2; }
+
 struct BigSmem {
   unsigned whist[kBigWarps][256];
   unsigned tstart[256];
@@ -404,7 +408,7 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
 }
 
 template <int CW>
-__global__ void __launch_bounds__(kBigBlock, 2) k_rf_big_items(BigArgs b) {
+__global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items(BigArgs b) {
   __shared__ BigSmem S;
   __shared__ float s_g[kBigBlock];
   __shared__ int s_p[kBigBlock];

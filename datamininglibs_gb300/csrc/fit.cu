@@ -447,9 +447,13 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     }
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-    int big_grid = 2 * sms;
+    int big_grid = big_ctas_per_sm(CW) * sms;  // one persistent CTA per resident slot
     if (slot_stride > 0) {
-      const long long budget = 16ll << 30;
+      // per-CTA scratch is 16 bytes per entry of the largest tree: at most 48 GB
+      // and a third of the free device memory
+      size_t free_b = 0, total_b = 0;
+      cudaMemGetInfo(&free_b, &total_b);
+      const long long budget = std::min<long long>(48ll << 30, (long long)free_b / 3);
       big_grid = (int)std::max(1ll, std::min<long long>(big_grid, budget / (16 * slot_stride)));
     }
     uint32_t* big_slot =
