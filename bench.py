@@ -313,6 +313,8 @@ def run_ours(args, w):
             dist.barrier()
         torch.cuda.synchronize()
 
+    # scheduling picked by the autotuner on an 8-tree sample (untimed)
+    tuning = dml.autotune(Xd, yd, sample_trees=8, stream=stream, **kw)
     for _ in range(args.warmup):
         dml.fit(Xd, yd, stream=stream, **kw).free()
     barrier()
@@ -433,7 +435,8 @@ def run_ours(args, w):
                    "max_depth": w["max_depth"], "min_leaf": w["min_leaf"],
                    "min_node_size": w["min_node_size"],
                    "l2": "inputs larger than L2 (%.0f MB of samples)" % (X.nbytes / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "tuning": tuning},
         "trees_per_s": world * args.steps * w["trees"] / (dev_ms / 1000.0),
         "nodes_per_fit": nodes / args.steps,
         "predict_rows_per_s": predict_rows_per_s,

@@ -7,6 +7,6 @@ This package binds it with ctypes.  There is no CPU fallback: loading fails
 loudly when the library is missing.
 """
 from .ensembles import (  # noqa: F401
-    DmlError, Forest, FitStats, OobStats, Server, accuracy, feature_importance, fit,
-    fit_batched, fit_plain, lib, oob_estimate, ALGO_RF, ALGO_ERT, CLASSIFICATION, REGRESSION,
+    DmlError, Forest, FitStats, OobStats, Server, accuracy, autotune, feature_importance, fit,
+    fit_batched, fit_plain, lib, oob_estimate, tuning_for, ALGO_RF, ALGO_ERT, CLASSIFICATION, REGRESSION,
 )

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdml_gb300.so")
 
-CUDA_SOURCES = ["fit.cu", "predict.cu", "server.cu", "oob.cu", "ranks.cu"] + [
+CUDA_SOURCES = ["fit.cu", "predict.cu", "server.cu", "oob.cu", "ranks.cu", "tuning.cu"] + [
     "search_cw%d.cu" % cw for cw in (1, 2, 4, 5, 8, 16)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -19,10 +19,6 @@ constexpr int kBigPer = 8;                       // elements per thread
 constexpr int kBigTile = kBigBlock * kBigPer;    // 2048
 constexpr int kBigWarps = kBigBlock / 32;
 
-// Resident CTAs per SM of the item kernel: three where the class counts are
-// narrow enough to fit 80 registers without spilling much, else two.
-constexpr int big_ctas_per_sm(int cw) { return cw <= 2 ? 3 : 2; }
-
 struct BigSmem {
   unsigned whist[kBigWarps][256];
   unsigned tstart[256];

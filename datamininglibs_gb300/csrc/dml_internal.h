@@ -7,6 +7,10 @@ namespace dml {
 constexpr int kMaxClasses = 32;
 constexpr int kMaxTries = 64;  // mandatory + optional tries evaluated per node
 
+// Resident CTAs per SM of the big-node item kernel: three where the packed
+// class counts (cw words) are narrow enough to fit 80 registers, else two.
+constexpr int big_ctas_per_sm(int cw) { return cw <= 2 ? 3 : 2; }
+
 // One forest of a fit batch (device-visible copy).
 struct ProbDesc {
   const float* X;          // feature-major [F * N]

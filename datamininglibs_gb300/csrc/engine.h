@@ -47,6 +47,20 @@ int quant_scale_from_max(float maxabs, long long n);
 
 dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s);
 
+// Largest RF node (entries) the shared-memory search kernel can hold.
+constexpr int kSearchSmemCap = 4096;
+
+// Scheduling of a fit (tuning.cu): RF nodes of up to warp_max entries (64, 128
+// or 256) are searched by a warp, up to smem_cap by a CTA in shared memory,
+// larger ones as per-try items on big_ctas persistent CTAs per SM.
+struct Tuning {
+  int warp_max, smem_cap, big_ctas;
+};
+int class_width(int n_classes);  // packed class-count words of the search kernels
+bool valid_tuning(const Tuning& t);
+Tuning default_tuning(int class_width);
+Tuning tuning_for(const dml_fit_desc* descs, int nprob, int class_width);
+
 // Stream-ordered device allocations from the device's memory pool.
 void* dev_alloc(size_t bytes, cudaStream_t s);
 void dev_free(void* p, cudaStream_t s);

@@ -296,7 +296,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     if (d.algo == DML_ALGO_RF) any_weights = true;
     if (d.task == DML_CLASSIFICATION) H_n = std::max(H_n, (long long)d.n_rows);
   }
-  const int CW = Cmax <= 2 ? 1 : Cmax <= 4 ? 2 : Cmax <= 8 ? 4 : Cmax <= 10 ? 5 : Cmax <= 16 ? 8 : 16;
+  const int CW = class_width(Cmax);
+  const Tuning tune = tuning_for(descs, nprob, CW);
   dml_fit_stats st;
   std::memset(&st, 0, sizeof(st));
 
@@ -443,11 +444,11 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     for (auto& P : hp) {
       max_mand = std::max(max_mand, P.n_mand);
       max_opt = std::max(max_opt, P.n_opt);
-      if (P.algo == DML_ALGO_RF && P.N > kSmemCap) slot_stride = std::max(slot_stride, P.N);
+      if (P.algo == DML_ALGO_RF && P.N > tune.smem_cap) slot_stride = std::max(slot_stride, P.N);
     }
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-    int big_grid = big_ctas_per_sm(CW) * sms;  // one persistent CTA per resident slot
+    int big_grid = tune.big_ctas * sms;  // persistent CTAs
     if (slot_stride > 0) {
       // per-CTA scratch is 16 bytes per entry of the largest tree: at most 48 GB
       // and a third of the free device memory
@@ -500,7 +501,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       Queues Q;
       for (int i = 0; i < kNumQ; ++i) Q.list[i] = qlist[i].p;
       Q.count = d_qcount;
-      Q.rf_small_cap = kSmemCap;
+      Q.rf_small_cap = tune.smem_cap;
+      Q.rf_warp_max = tune.warp_max;
       return Q;
     };
     if (any_weights) {
@@ -1106,6 +1108,7 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
     for (int i = 0; i < kNumQ; ++i) Q.list[i] = (int*)(A + oQueues) + (long long)i * kNaMaxSlots;
     Q.count = d_qcount;
     Q.rf_small_cap = kSmemCap;
+    Q.rf_warp_max = 256;
     if (d.algo == DML_ALGO_RF) {
       DML_CK(cudaMemsetAsync(wcnt, 0, sizeof(int) * total_slots, s));
       const int chunk = 1 << 16;

@@ -247,7 +247,8 @@ enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kQRfW2 = 4, kQRfW4 = 5
 struct Queues {
   int* list[kNumQ];
   int* count;  // [kNumQ]
-  int rf_small_cap;
+  int rf_small_cap;  // RF nodes up to this many entries sort in shared memory
+  int rf_warp_max;   // RF nodes up to this many entries (64, 128 or 256) sort in a warp
 };
 
 // Warp-aggregated append of `node` to queue q (all lanes call; `want` selects).
@@ -265,15 +266,17 @@ __device__ __forceinline__ void enqueue(Queues Q, int q, int node, bool want) {
   }
 }
 
-__device__ __forceinline__ int queue_of(const ProbDesc& P, int ecnt, int small_cap) {
+// The node class of a node with ecnt entries.  The RF thresholds come from
+// the fit's tuning; every class computes the same split.
+__device__ __forceinline__ int queue_of(const ProbDesc& P, int ecnt, const Queues& Q) {
   if (ecnt <= 8) return kQG8;
   if (ecnt <= 16) return kQG16;
   if (ecnt <= 32) return kQWarp;
   if (P.algo == 1) return kQErt;
-  if (ecnt <= 64) return kQRfW2;
-  if (ecnt <= 128) return kQRfW4;
-  if (ecnt <= 256) return kQRfW8;
-  return ecnt <= small_cap ? kQRfSmall : kQRfBig;
+  if (ecnt <= 64 && Q.rf_warp_max >= 64) return kQRfW2;
+  if (ecnt <= 128 && Q.rf_warp_max >= 128) return kQRfW4;
+  if (ecnt <= 256 && Q.rf_warp_max >= 256) return kQRfW8;
+  return ecnt <= Q.rf_small_cap ? kQRfSmall : kQRfBig;
 }
 
 __device__ __forceinline__ bool preleaf(const ProbDesc& P, int n, int depth) {
@@ -368,7 +371,7 @@ __global__ void __launch_bounds__(BLOCK) k_roots(const ProbDesc* probs, const in
   if (threadIdx.x < Cmax) cnt[(long long)gt * Cmax + threadIdx.x] = threadIdx.x < P.C ? s_cnt[threadIdx.x] : 0;
   if (threadIdx.x < 32) {
     bool want = threadIdx.x == 0 && !preleaf(P, (int)s_n, 0);
-    enqueue(Q, queue_of(P, out, Q.rf_small_cap), gt, want);
+    enqueue(Q, queue_of(P, out, Q), gt, want);
     if (want) {
       atomicAdd((unsigned long long*)&stats[0], (unsigned long long)out);
       atomicAdd((unsigned long long*)&stats[1], s_n);
@@ -525,8 +528,8 @@ __global__ void __launch_bounds__(256) k_emit(EmitArgs a) {
       cpR = cp + 1;
       wantL = !preleaf(P, L.n, L.depth);
       wantR = !preleaf(P, R.n, R.depth);
-      qL = queue_of(P, L.ecnt, a.Q.rf_small_cap);
-      qR = queue_of(P, R.ecnt, a.Q.rf_small_cap);
+      qL = queue_of(P, L.ecnt, a.Q);
+      qR = queue_of(P, R.ecnt, a.Q);
     } else {
       const long long lr = lb + (a.leafpos[j] - a.leafpos[fs]);
       cn.child_start = -1;

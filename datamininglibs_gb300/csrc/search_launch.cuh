@@ -10,7 +10,7 @@
 namespace dml {
 
 constexpr int kBlock = 256;
-constexpr int kSmemCap = 4096;  // RF nodes up to this many entries sort in shared memory
+constexpr int kSmemCap = kSearchSmemCap;  // RF nodes up to this many entries fit shared memory
 
 template <int CW>
 void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s);

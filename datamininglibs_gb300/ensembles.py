@@ -44,6 +44,11 @@ class FitDesc(ctypes.Structure):
                 ("tree_offset", ctypes.c_int32), ("balanced", ctypes.c_int32)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("warp_max", ctypes.c_int32), ("smem_cap", ctypes.c_int32),
+                ("big_ctas_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class OobStats(ctypes.Structure):
     _fields_ = [("pairs", ctypes.c_int64), ("pairs_correct", ctypes.c_int64),
                 ("pairs_sq_err", ctypes.c_double), ("rows", ctypes.c_int64),
@@ -101,6 +106,9 @@ _SIGS = {
     "dml_fit_plain": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_void_p]),
     "dml_last_fit_stats": (ctypes.c_int, [ctypes.POINTER(FitStats)]),
+    "dml_autotune": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.c_int32,
+                                    ctypes.POINTER(Tuning), ctypes.c_void_p]),
+    "dml_tuning_get": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.POINTER(Tuning)]),
     "dml_oob_estimate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FitDesc), ctypes.c_int32,
                                         ctypes.POINTER(OobStats), ctypes.c_void_p]),
     "dml_fit_noalloc": (ctypes.c_int, [ctypes.POINTER(FitDesc), ctypes.c_void_p, ctypes.c_int64,
@@ -321,6 +329,25 @@ def fit_batched(problems, stream=None):
     out = (ctypes.c_void_p * len(problems))()
     _check(lib().dml_fit_batched(len(problems), descs, out, _stream(stream)))
     return [Forest(out[i]) for i in range(len(problems))]
+
+
+def autotune(X, y, *, algo, task=CLASSIFICATION, n_trees=100, K=0, max_depth=1000,
+             min_node_size=5, min_leaf=1, n_classes=2, seed=0, sample_trees=8, stream=None):
+    """dml_autotune: times the scheduling candidates on the first sample_trees
+    trees of this problem and keeps the fastest for problems of its shape."""
+    d = _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed)
+    t = Tuning()
+    _check(lib().dml_autotune(ctypes.byref(d), sample_trees, ctypes.byref(t), _stream(stream)))
+    return {"warp_max": t.warp_max, "smem_cap": t.smem_cap, "big_ctas_per_sm": t.big_ctas_per_sm}
+
+
+def tuning_for(X, y, *, algo, task=CLASSIFICATION, n_trees=100, K=0, max_depth=1000,
+               min_node_size=5, min_leaf=1, n_classes=2, seed=0):
+    """dml_tuning_get: the scheduling a fit of this problem would use."""
+    d = _desc(X, y, algo, task, n_trees, K, max_depth, min_node_size, min_leaf, n_classes, seed)
+    t = Tuning()
+    _check(lib().dml_tuning_get(ctypes.byref(d), ctypes.byref(t)))
+    return {"warp_max": t.warp_max, "smem_cap": t.smem_cap, "big_ctas_per_sm": t.big_ctas_per_sm}
 
 
 def oob_estimate(forest, X, y, *, seed=0, tree_offset=0, balanced=0, permuted_feature=-1,

@@ -168,6 +168,27 @@ DML_API dml_status dml_fit_noalloc(const dml_fit_desc* desc, void* node_array,
 
 DML_API dml_status dml_last_fit_stats(dml_fit_stats* stats);
 
+/* Scheduling of RF fits (no counterpart in the reference): nodes of up to
+ * warp_max entries (64, 128 or 256) are searched by one warp, up to smem_cap
+ * entries (257 .. 4096) by one CTA in shared memory, larger ones as per-try
+ * items on big_ctas_per_sm persistent CTAs per SM.  Results do not depend on
+ * it.  dml_autotune fits the first sample_trees trees of desc once per
+ * candidate, keeps the fastest for desc's shape (algorithm, task, classes,
+ * log2 rows, log2 features, features tried) for later fits of that shape in
+ * this process, and appends it to the file named by the environment variable
+ * DML_TUNE_CACHE when set (read back by later processes).  dml_tuning_get
+ * gives the tuning a fit of desc would use. */
+typedef struct {
+  int32_t warp_max;
+  int32_t smem_cap;
+  int32_t big_ctas_per_sm;
+  int32_t reserved;
+} dml_tuning;
+
+DML_API dml_status dml_autotune(const dml_fit_desc* desc, int32_t sample_trees, dml_tuning* best,
+                                void* stream);
+DML_API dml_status dml_tuning_get(const dml_fit_desc* desc, dml_tuning* out);
+
 /* Out-of-bag estimate of an RF forest (gpurf.cu:290-359, kOobEstimate) and the
  * permutation run of one feature (gpurf.cu:361-438, kFeatureImp).  desc is the
  * descriptor the forest was fitted with (data, seed, tree_offset, balanced):

@@ -4,6 +4,7 @@
 // {offset/4 (64-bit), subsequence (64-bit)} with key = seed, and curand4()
 // returns the block of that counter, so for counter {c0, c1, c2, c3}:
 //   curand_init(seed, c2 | c3 << 32, 4 * (c0 | c1 << 32), &st); curand4(&st)
+// (for c1 < 2^30, where the offset fits 64 bits)
 // Prints the number of mismatching words; exit status 0 when there are none.
 #include <cstdio>
 #include <cstdlib>
@@ -45,8 +46,8 @@ int main() {
     if (i % 2 == 0)
       hc[i] = make_uint4((unsigned)(a % 100000), (unsigned)(a >> 60), (unsigned)(b % 4096),
                          (3u << 24) | (unsigned)(b >> 59));
-    else
-      hc[i] = make_uint4((unsigned)a, (unsigned)(a >> 32), (unsigned)b, (unsigned)(b >> 32));
+    else  // c1 < 2^30 so that the offset 4 * (c0 | c1 << 32) fits 64 bits
+      hc[i] = make_uint4((unsigned)a, (unsigned)(a >> 34), (unsigned)b, (unsigned)(b >> 32));
     hs[i] = i % 3 == 0 ? (unsigned long long)(i % 7) : next();
   }
   uint4* dc;
