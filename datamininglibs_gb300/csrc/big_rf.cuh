@@ -26,7 +26,7 @@ struct BigSmem {
   unsigned red[2 * kBigWarps];
   uint32_t tk[kBigTile];
   uint32_t tv[kBigTile];
-  unsigned long long scan64[kBigWarps];
+  unsigned long long scan64[kBigWarps * (kMaxClasses / 2 + 1)];  // block_excl_scan_n, CW + 1 values
   unsigned scan32[kBigWarps];
 };
 
@@ -291,22 +291,26 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
         ts += q[j] * (long long)w[j];
       }
     }
-    unsigned long long tot;
-    long long run_n = carry_n + (long long)block_excl_scan<kBigBlock, unsigned long long>(
-                                    (unsigned long long)tn, &tot, scan64);
-    carry_n += (long long)tot;
+    // one block scan of the row count and the packed class counts (or the
+    // regression sum) of every thread's elements
+    unsigned long long sv_[CW + 1], tot[CW + 1];
+    sv_[0] = (unsigned long long)tn;
+#pragma unroll
+    for (int c = 0; c < CW; ++c) sv_[1 + c] = P.task == 0 ? tl[c] : (c == 0 ? (unsigned long long)ts : 0ull);
+    block_excl_scan_n<kBigBlock, CW + 1>(sv_, tot, scan64);
+    long long run_n = carry_n + (long long)sv_[0];
+    carry_n += (long long)tot[0];
     long long run_s = 0;
     unsigned long long runL[CW];
     if (P.task == 0) {
 #pragma unroll
       for (int c = 0; c < CW; ++c) {
-        runL[c] = carry[c] + block_excl_scan<kBigBlock, unsigned long long>(tl[c], &tot, scan64);
-        carry[c] += tot;
+        runL[c] = carry[c] + sv_[1 + c];
+        carry[c] += tot[1 + c];
       }
     } else {
-      run_s = carry_s + (long long)block_excl_scan<kBigBlock, unsigned long long>(
-                            (unsigned long long)ts, &tot, scan64);
-      carry_s += (long long)tot;
+      run_s = carry_s + (long long)sv_[1];
+      carry_s += (long long)tot[1];
 #pragma unroll
       for (int c = 0; c < CW; ++c) runL[c] = 0;
     }
@@ -406,8 +410,8 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
 template <int CW>
 __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items(BigArgs b) {
   __shared__ BigSmem S;
-  __shared__ float s_g[kBigBlock];
-  __shared__ int s_p[kBigBlock];
+  __shared__ float s_g[kBigWarps];
+  __shared__ int s_p[kBigWarps];
   __shared__ ff s_prior;
   const LevelArgs& a = b.L;
   const int nnodes = b.phase == 1 ? b.nbig : *b.nretry;
@@ -470,23 +474,7 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     unsigned long long L[CW];
     big_boundary<CW>(k1, v1, packed, nullptr, wts, eq, m, nd, P, ncnt, a.H, s_prior, S.scan64, &g,
                      &p, &nl, &sl, L);
-    s_g[threadIdx.x] = g;
-    s_p[threadIdx.x] = p;
-    __syncthreads();
-    for (int s = kBigBlock / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) {
-        const float g2 = s_g[threadIdx.x + s];
-        const int p2 = s_p[threadIdx.x + s];
-        const float g1 = s_g[threadIdx.x];
-        const int p1 = s_p[threadIdx.x];
-        if (p2 >= 0 && (p1 < 0 || g2 > g1 || (g2 == g1 && p2 < p1))) {
-          s_g[threadIdx.x] = g2;
-          s_p[threadIdx.x] = p2;
-        }
-      }
-      __syncthreads();
-    }
-    const int bp = s_p[0];
+    const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
     if (bp >= 0 && p == bp) {
       Cand c;
       c.valid = 1;
@@ -607,9 +595,9 @@ template <int CW, int SMEM_CAP>
 __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
   __shared__ SortSmem<kBigBlock> SS;
   __shared__ unsigned red[2 * kBigWarps];
-  __shared__ unsigned long long scan64[kBigWarps];
-  __shared__ float s_g[kBigBlock];
-  __shared__ int s_p[kBigBlock];
+  __shared__ unsigned long long scan64[kBigWarps * (CW + 1)];
+  __shared__ float s_g[kBigWarps];
+  __shared__ int s_p[kBigWarps];
   __shared__ Cand s_cand, s_best;
   __shared__ int s_candL[kMaxClasses], s_bestL[kMaxClasses];
   __shared__ ff s_prior;
@@ -654,23 +642,7 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
       unsigned long long L[CW];
       big_boundary<CW>(k1, v1, packed, nullptr, wts, q_e, m, nd, P, ncnt, a.H, s_prior, scan64,
                        &g, &p, &nl, &sl, L);
-      s_g[threadIdx.x] = g;
-      s_p[threadIdx.x] = p;
-      __syncthreads();
-      for (int st = kBigBlock / 2; st > 0; st >>= 1) {
-        if (threadIdx.x < st) {
-          const float g2 = s_g[threadIdx.x + st];
-          const int p2 = s_p[threadIdx.x + st];
-          const float g1 = s_g[threadIdx.x];
-          const int p1 = s_p[threadIdx.x];
-          if (p2 >= 0 && (p1 < 0 || g2 > g1 || (g2 == g1 && p2 < p1))) {
-            s_g[threadIdx.x] = g2;
-            s_p[threadIdx.x] = p2;
-          }
-        }
-        __syncthreads();
-      }
-      const int bp = s_p[0];
+      const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
       if (bp >= 0 && p == bp) {
         Cand c;
         c.valid = 1;

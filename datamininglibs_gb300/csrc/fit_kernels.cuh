@@ -46,6 +46,86 @@ __device__ __forceinline__ T block_excl_scan(T v, T* total, T* sm) {
   return base + x - v;
 }
 
+// Exclusive block scans of NV 64-bit integers at once (one pair of barriers
+// for all of them); tot[j] receives the block total of value j.  sm holds
+// BLOCK/32 * NV words.  Integer sums, so the result is the same in any order.
+template <int BLOCK, int NV>
+__device__ __forceinline__ void block_excl_scan_n(unsigned long long (&v)[NV],
+                                                  unsigned long long (&tot)[NV],
+                                                  unsigned long long* sm) {
+  constexpr int NW = BLOCK / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long x[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    x[j] = v[j];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(kFull, x[j], o);
+      if (lane >= o) x[j] += y;
+    }
+  }
+  if (lane == 31)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) sm[w * NV + j] = x[j];
+  __syncthreads();
+  if (w == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      unsigned long long t = lane < NW ? sm[lane * NV + j] : 0ull;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(kFull, t, o);
+        if (lane >= o) t += y;
+      }
+      if (lane < NW) sm[lane * NV + j] = t;
+    }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    const unsigned long long base = w ? sm[(w - 1) * NV + j] : 0ull;
+    tot[j] = sm[(NW - 1) * NV + j];
+    v[j] = base + x[j] - v[j];
+  }
+  __syncthreads();
+}
+
+// The block's best boundary: valid (p >= 0) first, then the higher gain, then
+// the lower position -- a total order, so any reduction shape gives the same
+// winner.  Warp shuffles, one exchange of the warps' winners through sg / sp
+// (BLOCK/32 entries each), one barrier; every thread returns the position.
+// Callers separate a later reuse of sg / sp by a barrier.
+template <int BLOCK>
+__device__ __forceinline__ int block_best_pos(float g, int p, float* sg, int* sp) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float g2 = __shfl_xor_sync(kFull, g, o);
+    const int p2 = __shfl_xor_sync(kFull, p, o);
+    if (p2 >= 0 && (p < 0 || g2 > g || (g2 == g && p2 < p))) {
+      g = g2;
+      p = p2;
+    }
+  }
+  if (lane == 0) {
+    sg[w] = g;
+    sp[w] = p;
+  }
+  __syncthreads();
+  float bg = sg[0];
+  int bp = sp[0];
+#pragma unroll
+  for (int k = 1; k < BLOCK / 32; ++k) {
+    const float g2 = sg[k];
+    const int p2 = sp[k];
+    if (p2 >= 0 && (bp < 0 || g2 > bg || (g2 == bg && p2 < bp))) {
+      bg = g2;
+      bp = p2;
+    }
+  }
+  return bp;
+}
+
 template <class T>
 __device__ __forceinline__ T warp_excl_scan(T v) {
   const int lane = threadIdx.x & 31;
