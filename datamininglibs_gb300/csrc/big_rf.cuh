@@ -221,7 +221,7 @@ struct BigArgs {
 template <int CW>
 __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed, const int* elab,
                              const int* ew, const long long* eq, int m, const LNode& nd,
-                             const ProbDesc& P, const int* ncnt, const float2* H, ff prior,
+                             const ProbDesc& P, const int* ncnt, const long long* H, long long prior,
                              unsigned long long* scan64, float* out_g, int* out_p, long long* out_nl,
                              long long* out_sl, unsigned long long (&outL)[CW]) {
   const int C = P.C;
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
   __shared__ BigSmem S;
   __shared__ float s_g[kBigWarps];
   __shared__ int s_p[kBigWarps];
-  __shared__ ff s_prior;
+  __shared__ long long s_prior;
   const LevelArgs& a = b.L;
   const int nnodes = b.phase == 1 ? b.nbig : *b.nretry;
   const long long nitems = (long long)nnodes * b.tries_per_node;
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
   __shared__ int s_p[kBigWarps];
   __shared__ Cand s_cand, s_best;
   __shared__ int s_candL[kMaxClasses], s_bestL[kMaxClasses];
-  __shared__ ff s_prior;
+  __shared__ long long s_prior;
   __shared__ int s_scan[kBigWarps];
   __shared__ int s_next;
   extern __shared__ __align__(16) unsigned char dsm[];

@@ -137,52 +137,57 @@ __device__ __forceinline__ double pow2d(int e) {
 constexpr float kLn2f = 0.693147182464599609375f;
 constexpr float kSensible = 0.001f;  // gain > 1e-3 (double) <=> gain >= 0.001f
 
-__device__ __forceinline__ ff ld_ff(const float2* H, long long n) {
-  float2 v = __ldg(H + n);
-  return ff{v.x, v.y};
-}
+// Entropy terms in fixed point: H[n] = round(n ln n * 2^28) as int64 (built on
+// the host, the same table as the oracle's), so P and Q below are exact integer
+// sums in any order.  n < 2^27 keeps every sum below 2^63.
+constexpr float kHScale = 1.0f / 268435456.0f;  // 2^-28, exact
 
 // Prior numerator h(n) - sum_c h(N_c) of a node.
 template <class CountFn>
-__device__ __forceinline__ ff entropy_prior(const float2* H, long long n, int C, CountFn cnt) {
-  ff P = ld_ff(H, n);
-  for (int c = 0; c < C; ++c) P = ff_sub(P, ld_ff(H, cnt(c)));
+__device__ __forceinline__ long long entropy_prior(const long long* H, long long n, int C,
+                                                   CountFn cnt) {
+  long long P = __ldg(H + n);
+  for (int c = 0; c < C; ++c) P -= __ldg(H + cnt(c));
   return P;
 }
 
-// Entropy gain in bits of the split with left class counts L(c), node counts
-// Ntot(c): (prior - posterior) exactly as the oracle orders it.
-template <class LeftFn, class TotFn>
-__device__ __forceinline__ float entropy_gain(const float2* H, ff P, int C, long long nL,
-                                              long long nR, LeftFn L, TotFn Ntot) {
-  ff Q{0.0f, 0.0f};
-  Q = ff_add(Q, ld_ff(H, nL));
-  for (int c = 0; c < C; ++c) Q = ff_sub(Q, ld_ff(H, L(c)));
-  Q = ff_add(Q, ld_ff(H, nR));
-  for (int c = 0; c < C; ++c) Q = ff_sub(Q, ld_ff(H, Ntot(c) - L(c)));
-  ff D = ff_sub(P, Q);
-  float den = __fmul_rn(__ll2float_rn(nL + nR), kLn2f);
-  return __fdiv_rn(D.hi, den);
+// Gain in bits from the exact numerator D = P - Q of a node of n rows: the
+// float conversion of D, an exact power-of-two scale, n * ln2 and one division,
+// each rounded to nearest, as the oracle does.
+__device__ __forceinline__ float gain_from_numerator(long long D, long long n) {
+  const float num = __fmul_rn(__ll2float_rn(D), kHScale);
+  const float den = __fmul_rn(__ll2float_rn(n), kLn2f);
+  return __fdiv_rn(num, den);
 }
 
-// The same with the class loop unrolled to a compile-time bound CMAX >= C,
-// so that per-class counts held in registers are read without index
-// arithmetic.  Identical operation order.
+// Entropy gain in bits of the split with left class counts L(c), node counts
+// Ntot(c): Q = h(nL) + h(nR) - sum_c (h(L_c) + h(N_c - L_c)).
+template <class LeftFn, class TotFn>
+__device__ __forceinline__ float entropy_gain(const long long* H, long long P, int C,
+                                              long long nL, long long nR, LeftFn L,
+                                              TotFn Ntot) {
+  long long Q = __ldg(H + nL) + __ldg(H + nR);
+  for (int c = 0; c < C; ++c) {
+    const long long l = L(c);
+    Q -= __ldg(H + l) + __ldg(H + (Ntot(c) - l));
+  }
+  return gain_from_numerator(P - Q, nL + nR);
+}
+
+// The same with the class loop unrolled to a compile-time bound CMAX >= C, so
+// that per-class counts held in registers are read without index arithmetic.
 template <int CMAX, class LeftFn, class TotFn>
-__device__ __forceinline__ float entropy_gain_u(const float2* H, ff P, int C, long long nL,
-                                                long long nR, LeftFn L, TotFn Ntot) {
-  ff Q{0.0f, 0.0f};
-  Q = ff_add(Q, ld_ff(H, nL));
+__device__ __forceinline__ float entropy_gain_u(const long long* H, long long P, int C,
+                                                long long nL, long long nR, LeftFn L,
+                                                TotFn Ntot) {
+  long long Q = __ldg(H + nL) + __ldg(H + nR);
 #pragma unroll
   for (int c = 0; c < CMAX; ++c)
-    if (c < C) Q = ff_sub(Q, ld_ff(H, L(c)));
-  Q = ff_add(Q, ld_ff(H, nR));
-#pragma unroll
-  for (int c = 0; c < CMAX; ++c)
-    if (c < C) Q = ff_sub(Q, ld_ff(H, Ntot(c) - L(c)));
-  ff D = ff_sub(P, Q);
-  float den = __fmul_rn(__ll2float_rn(nL + nR), kLn2f);
-  return __fdiv_rn(D.hi, den);
+    if (c < C) {
+      const long long l = L(c);
+      Q -= __ldg(H + l) + __ldg(H + (Ntot(c) - l));
+    }
+  return gain_from_numerator(P - Q, nL + nR);
 }
 
 __device__ __forceinline__ float variance_gain(long long nL, long long SL, long long nR,

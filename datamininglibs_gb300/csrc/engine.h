@@ -40,8 +40,8 @@ struct CudaError {
 
 struct InvalidArg {};
 
-// n*ln(n) table recipe (host, IEEE double, fixed order) -> float pairs.
-void build_nlogn_table(long long nmax, float2* out);
+// n*ln(n) table recipe (host, IEEE double, fixed order) -> int64 fixed point 2^-28.
+void build_nlogn_table(long long nmax, long long* out);
 // Fixed-point scale of regression targets from max |y| and the row count.
 int quant_scale_from_max(float maxabs, long long n);
 

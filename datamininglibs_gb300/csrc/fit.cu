@@ -67,17 +67,10 @@ static double table_ln(double x) {
   return 2.0 * sum + (double)e * 0.6931471805599453094;
 }
 
-void build_nlogn_table(long long nmax, float2* out) {
-  for (long long n = 0; n <= nmax; ++n) {
-    if (n < 2) {
-      out[n] = make_float2(0.0f, 0.0f);
-      continue;
-    }
-    double h = (double)n * table_ln((double)n);
-    float hi = (float)h;
-    float lo = (float)(h - (double)hi);
-    out[n] = make_float2(hi, lo);
-  }
+// H[n] = round(n ln n * 2^28) (ldexp is exact; llrint rounds to nearest even).
+void build_nlogn_table(long long nmax, long long* out) {
+  for (long long n = 0; n <= nmax; ++n)
+    out[n] = n < 2 ? 0 : std::llrint(std::ldexp((double)n * table_ln((double)n), 28));
 }
 
 int quant_scale_from_max(float mx, long long n) {
@@ -147,21 +140,21 @@ constexpr int kPlainChunk = 512;  // reference: max_blocks_ / max_nominal_ nodes
 
 // n*ln(n) table cached on the device across fits (grow-only).
 struct TableCache {
-  float2* H = nullptr;
+  long long* H = nullptr;
   long long n = -1;
   std::mutex mu;
 };
 static TableCache g_table;
 
-static const float2* nlogn_table(long long nmax, cudaStream_t s) {
+static const long long* nlogn_table(long long nmax, cudaStream_t s) {
   std::lock_guard<std::mutex> lk(g_table.mu);
   if (g_table.n >= nmax) return g_table.H;
   long long n = std::max(nmax, (long long)1024);
-  std::vector<float2> h((size_t)n + 1);
+  std::vector<long long> h((size_t)n + 1);
   build_nlogn_table(n, h.data());
-  float2* d = nullptr;
-  DML_CK(cudaMalloc(&d, sizeof(float2) * (n + 1)));
-  DML_CK(cudaMemcpyAsync(d, h.data(), sizeof(float2) * (n + 1), cudaMemcpyHostToDevice, s));
+  long long* d = nullptr;
+  DML_CK(cudaMalloc(&d, sizeof(long long) * (n + 1)));
+  DML_CK(cudaMemcpyAsync(d, h.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, s));
   DML_CK(cudaStreamSynchronize(s));
   if (g_table.H) cudaFree(g_table.H);
   g_table.H = d;
@@ -430,7 +423,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
         }
       }
     }
-    const float2* H = H_n > 0 ? nlogn_table(H_n, s) : nullptr;
+    const long long* H = H_n > 0 ? nlogn_table(H_n, s) : nullptr;
 
     // --------------------------------------------------------- entries
     int* rowsA = (int*)alloc(sizeof(int) * total_slots);
@@ -942,7 +935,7 @@ constexpr int kMaxDevices = 64;
 static unsigned char* g_arena_dev[kMaxDevices];
 static std::mutex g_arena_mu;
 // host-side staging of the few values the driver reads back or uploads
-static float2 g_h_table[kNaMaxRows + 1];
+static long long g_h_table[kNaMaxRows + 1];
 static int g_h_tree_prob[kNaMaxSlots];
 
 // The array's device address on the current device (looked up once per device).
@@ -1067,12 +1060,12 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
         d.targets, P.N, P.task, P.S, P.lab == nullptr ? nullptr : (int*)(A + oLab),
         (long long*)(A + oQ));
     DML_CK(cudaGetLastError());
-    const float2* H = nullptr;
+    const long long* H = nullptr;
     if (P.task == 0) {
       build_nlogn_table(P.N, g_h_table);
-      DML_CK(cudaMemcpyAsync(A + oH, g_h_table, sizeof(float2) * (P.N + 1),
+      DML_CK(cudaMemcpyAsync(A + oH, g_h_table, sizeof(long long) * (P.N + 1),
                              cudaMemcpyHostToDevice, s));
-      H = (const float2*)(A + oH);
+      H = (const long long*)(A + oH);
     }
     ProbDesc* d_probs = (ProbDesc*)(A + oProb);
     DML_CK(cudaMemcpyAsync(d_probs, &P, sizeof(ProbDesc), cudaMemcpyHostToDevice, s));

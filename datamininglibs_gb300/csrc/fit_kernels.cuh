@@ -263,7 +263,7 @@ struct LevelArgs {
   int* wB;
   uint2* scratch;       // two pair buffers per entry slot: scratch[slot], scratch[slot + total]
   long long scratch_half;
-  const float2* H;      // n*ln(n) table
+  const long long* H;   // n*ln(n) table, fixed point 2^-28
   long long* stats;     // [2] += tries evaluated x node entries, [3] += node entries
 };
 
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
   __shared__ Cand s_best;
   __shared__ int s_phase;  // 0 stop, 1 run optional chunk
   __shared__ int s_scan[NW];
-  __shared__ ff s_prior;
+  __shared__ long long s_prior;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int wi = blockIdx.x; wi < a.nwork; wi += gridDim.x) {
     const int node = a.work[wi];
@@ -581,8 +581,8 @@ __device__ void cta_radix_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t*
 template <int BLOCK, int CW>
 __device__ void cta_best_boundary(const uint32_t* sk, const uint32_t* sv, int m, const LNode& nd,
                                   const ProbDesc& P, const int* ncnt, const int* lw_lab,
-                                  const int* lw_w, const long long* vq, const float2* H,
-                                  ff prior, Cand* cand, int* candL, int f, const float* xf,
+                                  const int* lw_w, const long long* vq, const long long* H,
+                                  long long prior, Cand* cand, int* candL, int f, const float* xf,
                                   const int* rows, unsigned long long* sm64, int* sm_bestpos,
                                   float* sm_bestg, unsigned long long* carry) {
   const int C = P.C;
@@ -732,7 +732,7 @@ __global__ void __launch_bounds__(BLOCK) k_rf_cta(LevelArgs a, int big) {
   __shared__ unsigned long long carry[2 * 16 + 2];
   __shared__ Cand s_cand, s_best;
   __shared__ int s_candL[kMaxClasses], s_bestL[kMaxClasses];
-  __shared__ ff s_prior;
+  __shared__ long long s_prior;
   __shared__ int s_scan[BLOCK / 32];
   __shared__ int s_next;
   extern __shared__ __align__(16) unsigned char dsm[];

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256, 2) k_group_nodes(LevelArgs a) {
     const int w = valid ? (a.wA ? __ldg(a.wA + nd.ebeg + gl) : 1) : 0;
     const int k = (valid && P.task == 0) ? __ldg(P.lab + row) : -1;
     const long long qv = (valid && P.task == 1) ? __ldg(P.q + row) : 0;
-    ff prior{0.0f, 0.0f};
+    long long prior = 0;
     int Nt[2 * CW];
 #pragma unroll
     for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;

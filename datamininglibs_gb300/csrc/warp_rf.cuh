@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
       }
     }
     __syncwarp();
-    ff prior{0.0f, 0.0f};
+    long long prior = 0;
     int Nt[2 * CW];
 #pragma unroll
     for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;

@@ -128,22 +128,18 @@ struct FF {
   float hi, lo;
 };
 
-std::vector<FF> build_nlogn_table(int64_t nmax) {
-  std::vector<FF> t((size_t)nmax + 1);
-  for (int64_t n = 0; n <= nmax; ++n) {
-    if (n < 2) {
-      t[n].hi = 0.0f;
-      t[n].lo = 0.0f;
-      continue;
-    }
-    double h = (double)n * table_ln((double)n);
-    float hi = (float)h;
-    float lo = (float)(h - (double)hi);
-    t[n].hi = hi;
-    t[n].lo = lo;
-  }
+// Entropy terms n ln n in fixed point: H[n] = round(n ln n * 2^28) (ldexp is
+// exact, llrint rounds to nearest even), so the sums of a gain (the prior
+// P = H[n] - sum_c H[N_c] and Q = H[nL] + H[nR] - sum_c (H[L_c] + H[R_c]),
+// gpudte.cu:76-117 restated) are exact integers; n < 2^27 keeps them below 2^63.
+std::vector<int64_t> build_nlogn_table(int64_t nmax) {
+  std::vector<int64_t> t((size_t)nmax + 1);
+  for (int64_t n = 0; n <= nmax; ++n)
+    t[n] = n < 2 ? 0 : std::llrint(std::ldexp((double)n * table_ln((double)n), 28));
   return t;
 }
+const float kHScale = 1.0f / 268435456.0f;  // 2^-28, exact
+
 
 // ------------------------------------------------------ float-float arithmetic
 inline FF fast_two_sum(float a, float b) {
@@ -213,6 +209,15 @@ inline double pow2d(int e) {  // exact 2^e for e in [-1022, 1023]
 }
 
 const float kLn2f = 0.693147182464599609375f;
+// Gain in bits from the exact numerator D = P - Q of a node of n rows: three
+// float roundings (the conversion of D, n * ln2, the division); the power-of-two
+// scale is exact.
+inline float gain_from_numerator(int64_t D, int64_t n) {
+  const float num = (float)D * kHScale;
+  const float den = (float)n * kLn2f;
+  return num / den;
+}
+
 const float kSensible = 0.001f;  // g > 1e-3 (double) <=> g >= 0.001f (float)
 
 // -------------------------------------------------------------- the problem
@@ -314,7 +319,7 @@ inline bool better(const Cand& a, const Cand& b) {
 
 struct Ctx {
   const Problem* p;
-  const std::vector<FF>* H;
+  const std::vector<int64_t>* H;
   std::vector<int32_t> lab;  // classification labels
   std::vector<int64_t> q;    // regression targets, fixed point 2^-S
   int S;
@@ -323,18 +328,14 @@ struct Ctx {
 
 double h64(double x) { return x <= 1.0 ? 0.0 : x * std::log(x); }
 
-float entropy_gain(const Ctx& cx, const FF& P, const int64_t* L, const int64_t* R,
+float entropy_gain(const Ctx& cx, int64_t P, const int64_t* L, const int64_t* R,
                    int C, int64_t nL, int64_t nR, double* g64,
                    const int64_t* Ntot) {
-  const std::vector<FF>& H = *cx.H;
-  FF Q{0.0f, 0.0f};
-  Q = ff_add(Q, H[nL]);
-  for (int c = 0; c < C; ++c) Q = ff_sub(Q, H[L[c]]);
-  Q = ff_add(Q, H[nR]);
-  for (int c = 0; c < C; ++c) Q = ff_sub(Q, H[R[c]]);
-  FF D = ff_sub(P, Q);
+  const std::vector<int64_t>& H = *cx.H;
+  int64_t Q = H[nL] + H[nR];
+  for (int c = 0; c < C; ++c) Q -= H[L[c]] + H[R[c]];
   int64_t n = nL + nR;
-  float g = D.hi / ((float)n * kLn2f);
+  float g = gain_from_numerator(P - Q, n);
   if (g64) {
     double num = h64((double)n) - h64((double)nL) - h64((double)nR);
     for (int c = 0; c < C; ++c)
@@ -378,7 +379,7 @@ struct OpenNode {
 
 // Evaluate one try.  Returns the candidate.
 Cand eval_try(const Ctx& cx, const std::vector<Entry>& E, const OpenNode& nd,
-              int tree, int depth, int idx, int tr, int f, const FF& P,
+              int tree, int depth, int idx, int tr, int f, int64_t P,
               std::vector<std::pair<uint32_t, int32_t>>& sortbuf) {
   const Problem& p = *cx.p;
   const int C = p.n_classes;
@@ -542,10 +543,10 @@ void fit_node(const Ctx& cx, int tree, int depth, size_t idx, OpenNode& nd,
   no.gain64 = NAN;
   Cand best{false, -FLT_MAX, -1, 0.0f, 0.0};
   if (nd.n > p.min_node_size && depth < p.max_depth) {
-    FF P{0.0f, 0.0f};
+    int64_t P = 0;
     if (p.task == 0) {
       P = (*cx.H)[nd.n];
-      for (int c = 0; c < C; ++c) P = ff_sub(P, (*cx.H)[nd.counts[c]]);
+      for (int c = 0; c < C; ++c) P -= (*cx.H)[nd.counts[c]];
     }
     // try loop: gpuert.cu:144-149 / gpurf.cu:177-182
     int K = p.K, F = p.F;
@@ -693,12 +694,9 @@ void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]
   for (int i = 0; i < 4; ++i) out[i] = w.v[i];
 }
 
-void oracle_nlogn_table(int64_t nmax, float* hi, float* lo) {
-  std::vector<FF> t = build_nlogn_table(nmax);
-  for (int64_t i = 0; i <= nmax; ++i) {
-    hi[i] = t[i].hi;
-    lo[i] = t[i].lo;
-  }
+void oracle_nlogn_table(int64_t nmax, int64_t* out) {
+  std::vector<int64_t> t = build_nlogn_table(nmax);
+  std::memcpy(out, t.data(), sizeof(int64_t) * (size_t)(nmax + 1));
 }
 
 // Entropy gain (bits) of a 2 x C count table, FP32 (table-based) and FP64.
@@ -711,13 +709,13 @@ float oracle_entropy_gain(const int64_t* L, const int64_t* R, int C,
     nR += R[c];
     Nt[c] = L[c] + R[c];
   }
-  std::vector<FF> H = build_nlogn_table(nL + nR);
+  std::vector<int64_t> H = build_nlogn_table(nL + nR);
   Ctx cx;
   cx.H = &H;
   cx.p = nullptr;
   cx.S = 0;
-  FF P = H[nL + nR];
-  for (int c = 0; c < C; ++c) P = ff_sub(P, H[Nt[c]]);
+  int64_t P = H[nL + nR];
+  for (int c = 0; c < C; ++c) P -= H[Nt[c]];
   return entropy_gain(cx, P, L, R, C, nL, nR, g64, Nt.data());
 }
 
@@ -778,7 +776,7 @@ void* oracle_fit(const oracle_desc* d) {
   Ctx cx;
   cx.p = &p;
   if (p.balanced) cx.class_rows = class_rows(p.y, p.N, p.n_classes);
-  std::vector<FF> H;
+  std::vector<int64_t> H;
   if (p.task == 0) {
     H = build_nlogn_table(p.N);
     cx.lab.resize((size_t)p.N);

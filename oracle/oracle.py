@@ -47,7 +47,7 @@ def lib():
                                      ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
                                      ctypes.c_void_p, ctypes.c_int]
         L.oracle_philox.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-        L.oracle_nlogn_table.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_nlogn_table.argtypes = [ctypes.c_int64, ctypes.c_void_p]
         L.oracle_entropy_gain.restype = ctypes.c_float
         L.oracle_entropy_gain.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_double)]
@@ -152,10 +152,10 @@ def philox(ctr, key):
 
 
 def nlogn_table(nmax):
-    hi = np.zeros(nmax + 1, np.float32)
-    lo = np.zeros(nmax + 1, np.float32)
-    lib().oracle_nlogn_table(nmax, hi.ctypes.data, lo.ctypes.data)
-    return hi, lo
+    """H[n] = round(n ln n * 2^28) as int64, n = 0..nmax (the gain table)."""
+    out = np.zeros(nmax + 1, np.int64)
+    lib().oracle_nlogn_table(nmax, out.ctypes.data)
+    return out
 
 
 def entropy_gain(L, R):

@@ -23,12 +23,14 @@ def test_philox_known_answers():
 
 
 def test_nlogn_table_accuracy():
-    hi, lo = oracle.nlogn_table(100000)
+    """Fixed point 2^-28: every entry within half a unit (plus double rounding)
+    of n ln n."""
+    H = oracle.nlogn_table(100000)
     n = np.arange(2, 100001, dtype=np.float64)
     exact = n * np.log(n)
-    got = hi[2:].astype(np.float64) + lo[2:].astype(np.float64)
-    assert np.max(np.abs(got - exact) / exact) < 1e-13
-    assert hi[0] == 0 and hi[1] == 0
+    got = H[2:].astype(np.float64) / 2.0 ** 28
+    assert np.all(np.abs(got - exact) <= 2.0 ** -29 + 1e-15 * exact)
+    assert H[0] == 0 and H[1] == 0
 
 
 def test_entropy_against_reference(golden_dir):
@@ -37,7 +39,7 @@ def test_entropy_against_reference(golden_dir):
         g32, g64 = oracle.entropy_gain(L[:C], R[:C])
         # FP64 shadow == the reference's double instantiation
         assert abs(g64 - gd) <= 1e-12 * max(abs(gd), 1.0), (L[:C], R[:C])
-        # FP32 (float-float table) gain within 1e-6 relative of FP64 (+1e-7 bits floor)
+        # FP32 (fixed-point table) gain within 1e-6 relative of FP64 (+1e-7 bits floor)
         assert abs(g32 - gd) <= 1e-6 * abs(gd) + 1e-7, (L[:C], R[:C], g32, gd)
 
 
