@@ -13,6 +13,8 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "dml_internal.h"
+
 namespace dml {
 
 // ------------------------------------------------------------------ Philox
@@ -199,6 +201,28 @@ __device__ __forceinline__ float variance_gain(long long nL, long long SL, long 
   float w = __fdiv_rn(__fmul_rn(__ll2float_rn(nL), __ll2float_rn(nR)), __ll2float_rn(nL + nR));
   float g = ff_mul_f(d2, w).hi;
   return scale_pow2(g, -2 * S);
+}
+
+// Walks trees t0 .. t0+W-1 for one row in lockstep, so that W independent
+// node loads are in flight at a time; x(f) reads the row's value of feature f.
+// leaf[k] receives tree t0+k's leaf (predict layout, PNode).
+template <int W, class XFn>
+__device__ __forceinline__ void walk_trees(const PNode* __restrict__ nodes, int t0, XFn x,
+                                           int4 (&leaf)[W]) {
+#pragma unroll
+  for (int k = 0; k < W; ++k) leaf[k] = __ldg(reinterpret_cast<const int4*>(nodes) + t0 + k);
+  bool more = true;
+  while (more) {
+    more = false;
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+      if (leaf[k].x >= 0) {
+        const int nx = goes_left(x(leaf[k].y), __int_as_float(leaf[k].z)) ? leaf[k].x
+                                                                           : leaf[k].x + 1;
+        leaf[k] = __ldg(reinterpret_cast<const int4*>(nodes) + nx);
+        more |= leaf[k].x >= 0;
+      }
+  }
 }
 
 // Candidate order: valid first, then higher gain, lower feature, lower threshold.

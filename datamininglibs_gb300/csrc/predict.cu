@@ -23,9 +23,11 @@ void clear_error();
 void init_pool_once();
 
 constexpr int kPredBlock = 128;
+constexpr int kWalk = 4;  // trees walked in lockstep per thread
 
-// Rows are walked through all trees; a tile of the row's features is not
-// staged because each row reads only the features on its paths.
+// Rows are walked through all trees, four at a time; a tile of the row's
+// features is not staged because each row reads only the features on its
+// paths.
 template <int TASK>
 __global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict__ nodes,
                                                         int n_trees, int C,
@@ -39,17 +41,28 @@ __global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict_
     for (int c = 0; c < C; ++c) my[c] = 0;
   float acc = 0.0f;
   if (act) {
-    for (int t = 0; t < n_trees; ++t) {
-      int4 p = __ldg(reinterpret_cast<const int4*>(nodes) + t);
-      while (p.x >= 0) {
-        float x = __ldg(X + (long long)p.y * N + row);
-        int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
-        p = __ldg(reinterpret_cast<const int4*>(nodes) + nx);
+    auto xr = [&](int f) { return __ldg(X + (long long)f * N + row); };
+    // kWalk trees in lockstep (kWalk loads in flight), then the rest one by
+    // one; leaves are consumed in tree order, so regression sums keep it
+    int t = 0;
+    for (; t + kWalk <= n_trees; t += kWalk) {
+      int4 lf[kWalk];
+      walk_trees<kWalk>(nodes, t, xr, lf);
+#pragma unroll
+      for (int k = 0; k < kWalk; ++k) {
+        if (TASK == 0)
+          my[lf[k].y] += 1;
+        else
+          acc = __fadd_rn(acc, __int_as_float(lf[k].z));
       }
+    }
+    for (; t < n_trees; ++t) {
+      int4 lf[1];
+      walk_trees<1>(nodes, t, xr, lf);
       if (TASK == 0)
-        my[p.y] += 1;
+        my[lf[0].y] += 1;
       else
-        acc = __fadd_rn(acc, __int_as_float(p.z));
+        acc = __fadd_rn(acc, __int_as_float(lf[0].z));
     }
     if (TASK == 0) {
       for (int c = 0; c < C; ++c) out[row * C + c] = (float)my[c];

@@ -69,17 +69,26 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles(const PredTile* __r
     for (int c = 0; c < t.C; ++c) my[c] = 0;
   float acc = 0.0f;
   if (act) {
-    for (int k = 0; k < t.n_trees; ++k) {
-      int4 p = __ldg(reinterpret_cast<const int4*>(t.nodes) + k);
-      while (p.x >= 0) {
-        const float x = __ldg(t.X + (long long)p.y * t.n + row);
-        const int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
-        p = __ldg(reinterpret_cast<const int4*>(t.nodes) + nx);
+    auto xr = [&](int f) { return __ldg(t.X + (long long)f * t.n + row); };
+    int k = 0;
+    for (; k + 4 <= t.n_trees; k += 4) {  // four trees in lockstep, consumed in order
+      int4 lf[4];
+      walk_trees<4>(t.nodes, k, xr, lf);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (t.task == 0)
+          my[lf[j].y] += 1;
+        else
+          acc = __fadd_rn(acc, __int_as_float(lf[j].z));
       }
+    }
+    for (; k < t.n_trees; ++k) {
+      int4 lf[1];
+      walk_trees<1>(t.nodes, k, xr, lf);
       if (t.task == 0)
-        my[p.y] += 1;
+        my[lf[0].y] += 1;
       else
-        acc = __fadd_rn(acc, __int_as_float(p.z));
+        acc = __fadd_rn(acc, __int_as_float(lf[0].z));
     }
     if (t.task == 0)
       for (int c = 0; c < t.C; ++c) t.out[row * t.C + c] = (float)my[c];
