@@ -7,9 +7,10 @@ namespace dml {
 constexpr int kMaxClasses = 32;
 constexpr int kMaxTries = 64;  // mandatory + optional tries evaluated per node
 
-// Resident CTAs per SM of the big-node item kernel: three where the packed
-// class counts (cw words) are narrow enough to fit 80 registers, else two.
-constexpr int big_ctas_per_sm(int cw) { return cw <= 2 ? 3 : 2; }
+// Resident CTAs per SM of the big-node item kernel: three (80 registers, a
+// few hundred bytes of spills that the extra warps more than pay for) up to
+// 16 classes, two for wider class counts.
+constexpr int big_ctas_per_sm(int cw) { return cw <= 8 ? 3 : 2; }
 
 // One forest of a fit batch (device-visible copy).
 struct ProbDesc {

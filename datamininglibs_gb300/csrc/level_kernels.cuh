@@ -32,7 +32,9 @@ __device__ __forceinline__ T grp_sum(T v, unsigned gm) {
 }
 
 template <int CW, int G>
-__global__ void __launch_bounds__(256, 2) k_group_nodes(LevelArgs a) {
+// Three resident CTAs per SM (80 registers): the extra warps hide the shuffle
+// latency of the sort and scans better than 128 registers without spills.
+__global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
   constexpr int NPW = 32 / G;                 // nodes per warp
   constexpr int NS = (10 + G - 1) / G;        // ERT samples per lane
   const int lane = threadIdx.x & 31;
