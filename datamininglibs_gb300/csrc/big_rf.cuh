@@ -22,7 +22,7 @@ constexpr int kBigWarps = kBigBlock / 32;
 struct BigSmem {
   unsigned whist[kBigWarps][256];
   unsigned tstart[256];
-  unsigned running[256];
+  unsigned running[2][256];
   unsigned red[2 * kBigWarps];
   uint32_t tk[kBigTile];
   uint32_t tv[kBigTile];
@@ -36,16 +36,36 @@ __device__ __forceinline__ float key_value(const ProbDesc& P, int f, uint32_t k)
   return P.rank ? __ldg(P.vals + (long long)f * P.N + k) : from_orderable(k);
 }
 
+// Exclusive scan over the 256 digits of per-digit totals (thread d owns digit
+// d): warp shuffles, one exchange of warp sums, one barrier.  The caller
+// separates a later reuse of sm (kBigWarps words) by a barrier.
+static __device__ __forceinline__ unsigned digit_excl_scan(unsigned tot, unsigned* sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned x = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm[warp] = x;
+  __syncthreads();
+  unsigned ex = x - tot;
+  for (int w = 0; w < warp; ++w) ex += sm[w];
+  return ex;
+}
+
 // One LSD pass of pairs (kin, vin) -> (kout, vout) on byte `shift`.
 // Scratch written earlier in the same kernel is read with plain loads (never
 // the read-only cache path).
-static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout,
-                         int m, int shift, BigSmem& S) {
+static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                                uint32_t* vout, int m, int shift, BigSmem& S) {
+  static_assert(kBigBlock == 256, "one thread per digit");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int dg = threadIdx.x;
   const unsigned lt = (1u << lane) - 1u;
-  // global digit histogram
-  for (int i = threadIdx.x; i < kBigWarps * 256; i += kBigBlock) (&S.whist[0][0])[i] = 0;
-  __syncthreads();
+  // global digit histogram -> each digit's first output position
+  for (int i = lane; i < 256; i += 32) S.whist[warp][i] = 0;
+  __syncwarp();
   for (int base = 0; base < m; base += kBigTile) {
     uint32_t d[kBigPer];
 #pragma unroll
@@ -59,15 +79,15 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
   }
   __syncthreads();
   {
-    const int dg = threadIdx.x;  // kBigBlock == 256: one thread per digit
     unsigned tot = 0;
     for (int w = 0; w < kBigWarps; ++w) tot += S.whist[w][dg];
-    unsigned total;
-    unsigned ex = block_excl_scan<kBigBlock, unsigned>(tot, &total, S.scan32);
-    S.running[dg] = ex;
+    S.running[0][dg] = digit_excl_scan(tot, S.scan32);
   }
   __syncthreads();
-  // tiles: stable local sort in shared memory, contiguous run writes
+  // tiles: stable local sort in shared memory, contiguous run writes; the
+  // running positions are double-buffered (tile t reads running[cur] and
+  // writes running[cur ^ 1] for tile t + 1)
+  int cur = 0;
   for (int base = 0; base < m; base += kBigTile) {
     const int tn = min(kBigTile, m - base);
     const int wbeg = warp * 256;
@@ -78,8 +98,8 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
       k[r] = i < tn ? kin[base + i] : 0u;
       v[r] = i < tn ? vin[base + i] : 0u;
     }
-    for (int i = threadIdx.x; i < kBigWarps * 256; i += kBigBlock) (&S.whist[0][0])[i] = 0;
-    __syncthreads();
+    for (int i = lane; i < 256; i += 32) S.whist[warp][i] = 0;
+    __syncwarp();
     unsigned pr[kBigPer];  // each element's equal-digit lanes, reused by the scatter
 #pragma unroll
     for (int r = 0; r < kBigPer; ++r) {
@@ -88,27 +108,31 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
       const unsigned mask = __ballot_sync(kFull, act);
       pr[r] = 0;
       if (act) {
-        const unsigned dg = (k[r] >> shift) & 255u;
-        const unsigned peers = digit_peers(mask, dg);
+        const unsigned dgt = (k[r] >> shift) & 255u;
+        const unsigned peers = digit_peers(mask, dgt);
         pr[r] = peers;
-        if ((peers & lt) == 0) S.whist[warp][dg] += __popc(peers);
+        if ((peers & lt) == 0) S.whist[warp][dgt] += __popc(peers);
       }
       __syncwarp();
     }
     __syncthreads();
     {
-      const int dg = threadIdx.x;
+      unsigned h[kBigWarps];
       unsigned tot = 0;
-      for (int w = 0; w < kBigWarps; ++w) tot += S.whist[w][dg];
-      unsigned total;
-      unsigned ex = block_excl_scan<kBigBlock, unsigned>(tot, &total, S.scan32);
+#pragma unroll
+      for (int w = 0; w < kBigWarps; ++w) {
+        h[w] = S.whist[w][dg];
+        tot += h[w];
+      }
+      const unsigned ex = digit_excl_scan(tot, S.scan32);
       S.tstart[dg] = ex;
       unsigned run = ex;
+#pragma unroll
       for (int w = 0; w < kBigWarps; ++w) {
-        unsigned h = S.whist[w][dg];
         S.whist[w][dg] = run;
-        run += h;
+        run += h[w];
       }
+      S.running[cur ^ 1][dg] = S.running[cur][dg] + tot;
     }
     __syncthreads();
 #pragma unroll
@@ -117,31 +141,26 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
       const bool act = i < tn;
       const unsigned mask = __ballot_sync(kFull, act);
       if (act) {
-        const unsigned dg = (k[r] >> shift) & 255u;
+        const unsigned dgt = (k[r] >> shift) & 255u;
         const unsigned peers = pr[r];
-        const unsigned pos = S.whist[warp][dg] + __popc(peers & lt);
+        const unsigned pos = S.whist[warp][dgt] + __popc(peers & lt);
         S.tk[pos] = k[r];
         S.tv[pos] = v[r];
         __syncwarp(mask);
-        if ((peers & lt) == 0) S.whist[warp][dg] += __popc(peers);
+        if ((peers & lt) == 0) S.whist[warp][dgt] += __popc(peers);
       }
       __syncwarp();
     }
     __syncthreads();
     for (int j = threadIdx.x; j < tn; j += kBigBlock) {
       const uint32_t kk = S.tk[j];
-      const unsigned dg = (kk >> shift) & 255u;
-      const unsigned pos = S.running[dg] + (j - S.tstart[dg]);
+      const unsigned dgt = (kk >> shift) & 255u;
+      const unsigned pos = S.running[cur][dgt] + (j - S.tstart[dgt]);
       kout[pos] = kk;
       vout[pos] = S.tv[j];
     }
     __syncthreads();
-    if (threadIdx.x < 256) {
-      const int dg = threadIdx.x;
-      const unsigned end = dg == 255 ? (unsigned)tn : S.tstart[dg + 1];
-      S.running[dg] += end - S.tstart[dg];
-    }
-    __syncthreads();
+    cur ^= 1;
   }
 }
 

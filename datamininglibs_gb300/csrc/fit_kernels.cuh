@@ -480,29 +480,40 @@ struct SortSmem {
 template <int BLOCK>
 __device__ void radix_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                            uint32_t* vout, int m, int shift, SortSmem<BLOCK>& S) {
+  static_assert(BLOCK == 256, "one thread per digit");
   constexpr int NW = BLOCK / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int chunk = ((m + NW - 1) / NW + 31) & ~31;
   const int beg = min(m, warp * chunk), end = min(m, beg + chunk);
-  for (int i = threadIdx.x; i < NW * 256; i += BLOCK) (&S.hist[0][0])[i] = 0;
-  __syncthreads();
+  // each warp clears and fills its own histogram row
+  for (int i = lane; i < 256; i += 32) S.hist[warp][i] = 0;
+  __syncwarp();
   for (int i = beg + lane; i < end; i += 32) atomicAdd(&S.hist[warp][(kin[i] >> shift) & 255u], 1u);
   __syncthreads();
-  // digit-major, warp-minor exclusive offsets
+  // digit-major, warp-minor exclusive offsets; thread d owns digit d
   {
     const int d = threadIdx.x;
+    unsigned h[NW];
     unsigned tot = 0;
-    if (d < 256)
-      for (int w = 0; w < NW; ++w) tot += S.hist[w][d];
-    unsigned total;
-    unsigned base = block_excl_scan<BLOCK, unsigned>(d < 256 ? tot : 0u, &total, S.scan_tmp);
-    if (d < 256) {
-      unsigned run = base;
-      for (int w = 0; w < NW; ++w) {
-        unsigned h = S.hist[w][d];
-        S.hist[w][d] = run;
-        run += h;
-      }
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      h[w] = S.hist[w][d];
+      tot += h[w];
+    }
+    unsigned x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) S.scan_tmp[warp] = x;
+    __syncthreads();
+    unsigned run = x - tot;
+    for (int w = 0; w < warp; ++w) run += S.scan_tmp[w];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      S.hist[w][d] = run;
+      run += h[w];
     }
   }
   __syncthreads();
