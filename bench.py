@@ -218,16 +218,30 @@ def batched_leg(dml, torch, stream):
 def serve_leg(dml, torch, stream, c2_forest, c4_forests, c4_probs):
     """Resident forests (the ERT binary, RF multiclass and RF regression
     workloads plus 32 of the uneven forests), Poisson arrivals at 100k req/s
-    offered, request rows log-uniform in [1, 65536], forest chosen uniformly."""
+    offered, request rows log-uniform in [1, 65536], forest chosen uniformly.
+    Also returns the device time of the ERT binary and RF regression fits
+    (their samples resident, after one untimed fit)."""
     from datamininglibs_gb300 import synth
+
+    def timed_fit(X, y, **kw):  # device-resident samples; a second, timed fit
+        Xd, yd = torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda()
+        dml.fit(Xd, yd, stream=stream, **kw).free()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        f = dml.fit(Xd, yd, stream=stream, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        return f, {"ms": ms, "nodes": f.info().n_nodes,
+                   "nodes_per_s": f.info().n_nodes / (ms / 1000.0)}
     X1, y1 = synth.ert_binary()
-    f1 = dml.fit(X1, y1, algo=1, n_trees=64, K=7, max_depth=12, min_node_size=10, n_classes=2,
-                 seed=0)
+    f1, fit1 = timed_fit(X1, y1, algo=1, n_trees=64, K=7, max_depth=12, min_node_size=10,
+                         n_classes=2, seed=0)
     X3, y3 = synth.rf_regression()
-    f3 = dml.fit(torch.from_numpy(X3).cuda(), torch.from_numpy(y3).cuda(), algo=0, task=1,
-                 n_trees=64, K=21, max_depth=24, min_node_size=5, min_leaf=5, seed=0,
-                 stream=stream)
+    f3, fit3 = timed_fit(X3, y3, algo=0, task=1, n_trees=64, K=21, max_depth=24,
+                         min_node_size=5, min_leaf=5, seed=0)
     del X3, y3
+    configs = {"ert_binary_4601x57_64trees_fit": fit1, "rf_regression_4Mx64_64trees_fit": fit3}
     forests = [(f1, "ert_binary"), (c2_forest, "rf_multiclass"), (f3, "rf_regression")]
     forests += [(f, "normal") for f in c4_forests]
     rng = np.random.default_rng(5)
@@ -286,7 +300,7 @@ def serve_leg(dml, torch, stream, c2_forest, c4_forests, c4_probs):
             "p50_ms_le4k": float(np.percentile(lat[small], 50)),
             "p99_ms_le4k": float(np.percentile(lat[small], 99)),
             "launches": st.launches, "plain_rows_per_s": plain_rows_per_s,
-            "speedup_vs_plain": st.rows_per_s / plain_rows_per_s}
+            "speedup_vs_plain": st.rows_per_s / plain_rows_per_s}, configs
 
 
 def run_ours(args, w):
@@ -314,7 +328,7 @@ def run_ours(args, w):
         torch.cuda.synchronize()
 
     # scheduling picked by the autotuner on an 8-tree sample (untimed)
-    tuning = dml.autotune(Xd, yd, sample_trees=8, stream=stream, **kw)
+    tuning = None if args.no_tune else dml.autotune(Xd, yd, sample_trees=8, stream=stream, **kw)
     for _ in range(args.warmup):
         dml.fit(Xd, yd, stream=stream, **kw).free()
     barrier()
@@ -403,7 +417,8 @@ def run_ours(args, w):
         extras["plain_path"] = {"nodes_per_s": fp.info().n_nodes / (time.perf_counter() - tp)}
         fp.free()
         extras["batched_uneven"], c4f, c4p = batched_leg(dml, torch, stream)
-        extras["serve"] = serve_leg(dml, torch, stream, last_forest, c4f, c4p)
+        extras["serve"], extras["other_configs"] = serve_leg(dml, torch, stream, last_forest,
+                                                             c4f, c4p)
         for f in c4f:
             f.free()
     last_forest.free()
@@ -475,6 +490,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="a reduced workload for quick checks")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner (default scheduling; for ncu launch indices)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-path, batched-forest and serving legs")
     args = ap.parse_args()
