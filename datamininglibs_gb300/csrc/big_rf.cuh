@@ -28,7 +28,23 @@ struct BigSmem {
   uint32_t tv[kBigTile];
   unsigned long long scan64[kBigWarps * (kMaxClasses / 2 + 1)];  // block_excl_scan_n, CW + 1 values
   unsigned scan32[kBigWarps];
+  unsigned dh[4][256];  // per-digit histograms of the item's keys, counted while gathering
 };
+
+// Adds one warp-round of digits to a histogram: every lane of the warp calls,
+// `act` lanes contribute.  A round whose active lanes share one digit (a
+// constant byte) adds with one atomic instead of 32 on the same word.
+__device__ __forceinline__ void hist_add_round(unsigned* h, unsigned dgt, bool act) {
+  const unsigned mask = __ballot_sync(kFull, act);
+  if (mask == 0) return;
+  const int src = __ffs(mask) - 1;
+  const unsigned d0 = __shfl_sync(kFull, dgt, src);
+  if (__all_sync(kFull, !act || dgt == d0)) {
+    if ((int)(threadIdx.x & 31) == src) atomicAdd(&h[d0], (unsigned)__popc(mask));
+  } else if (act) {
+    atomicAdd(&h[dgt], 1u);
+  }
+}
 
 // The value of a sort key of feature f: a rank (looked up) or an orderable key.
 // Equal to from_orderable of the value's key either way (-0 reads as +0).
@@ -54,35 +70,18 @@ static __device__ __forceinline__ unsigned digit_excl_scan(unsigned tot, unsigne
   return ex;
 }
 
-// One LSD pass of pairs (kin, vin) -> (kout, vout) on byte `shift`.
-// Scratch written earlier in the same kernel is read with plain loads (never
-// the read-only cache path).
+// One LSD pass of pairs (kin, vin) -> (kout, vout) on byte `shift`, whose
+// digit histogram over all m keys is dh.  Scratch written earlier in the same
+// kernel is read with plain loads (never the read-only cache path).
 static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
-                                uint32_t* vout, int m, int shift, BigSmem& S) {
+                                uint32_t* vout, int m, int shift, const unsigned* dh,
+                                BigSmem& S) {
   static_assert(kBigBlock == 256, "one thread per digit");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int dg = threadIdx.x;
   const unsigned lt = (1u << lane) - 1u;
-  // global digit histogram -> each digit's first output position
-  for (int i = lane; i < 256; i += 32) S.whist[warp][i] = 0;
-  __syncwarp();
-  for (int base = 0; base < m; base += kBigTile) {
-    uint32_t d[kBigPer];
-#pragma unroll
-    for (int j = 0; j < kBigPer; ++j) {
-      const int i = base + j * kBigBlock + threadIdx.x;
-      d[j] = i < m ? (kin[i] >> shift) & 255u : 256u;
-    }
-#pragma unroll
-    for (int j = 0; j < kBigPer; ++j)
-      if (d[j] < 256u) atomicAdd(&S.whist[warp][d[j]], 1u);
-  }
-  __syncthreads();
-  {
-    unsigned tot = 0;
-    for (int w = 0; w < kBigWarps; ++w) tot += S.whist[w][dg];
-    S.running[0][dg] = digit_excl_scan(tot, S.scan32);
-  }
+  // each digit's first output position
+  S.running[0][dg] = digit_excl_scan(dh[dg], S.scan32);
   __syncthreads();
   // tiles: stable local sort in shared memory, contiguous run writes; the
   // running positions are double-buffered (tile t reads running[cur] and
@@ -164,55 +163,23 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
   }
 }
 
-// Sorts (k, v) of length m; the result ends in (k, v).  Passes whose byte is
-// the same in every key are skipped.
-static __device__ void big_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2, int m,
-                         BigSmem& S) {
-  unsigned o = 0, an = 0xFFFFFFFFu;
-  for (int base = 0; base < m; base += kBigTile) {
-#pragma unroll
-    for (int j = 0; j < kBigPer; ++j) {
-      const int i = base + j * kBigBlock + threadIdx.x;
-      if (i < m) {
-        const uint32_t x = k[i];
-        o |= x;
-        an &= x;
-      }
-    }
-  }
-  for (int s = 16; s > 0; s >>= 1) {
-    o |= __shfl_xor_sync(kFull, o, s);
-    an &= __shfl_xor_sync(kFull, an, s);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    S.red[2 * (threadIdx.x >> 5)] = o;
-    S.red[2 * (threadIdx.x >> 5) + 1] = an;
-  }
-  __syncthreads();
-  unsigned oo = 0, aa = 0xFFFFFFFFu;
-  for (int w = 0; w < kBigWarps; ++w) {
-    oo |= S.red[2 * w];
-    aa &= S.red[2 * w + 1];
-  }
-  const unsigned diff = oo ^ aa;
-  __syncthreads();
+// Sorts (k, v) of length m whose varying key bits are `diff` and whose digit
+// histograms are S.dh.  Passes whose byte is the same in every key are
+// skipped; returns true when the result is in (k2, v2), false when in (k, v).
+static __device__ bool big_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2, int m,
+                                unsigned diff, BigSmem& S) {
   bool primary = true;
-  for (int shift = 0; shift < 32; shift += 8) {
+  for (int d = 0; d < 4; ++d) {
+    const int shift = 8 * d;
     if (((diff >> shift) & 255u) == 0) continue;
     if (primary)
-      big_pass(k, v, k2, v2, m, shift, S);
+      big_pass(k, v, k2, v2, m, shift, S.dh[d], S);
     else
-      big_pass(k2, v2, k, v, m, shift, S);
+      big_pass(k2, v2, k, v, m, shift, S.dh[d], S);
     primary = !primary;
     __syncthreads();
   }
-  if (!primary) {
-    for (int i = threadIdx.x; i < m; i += kBigBlock) {
-      k[i] = k2[i];
-      v[i] = v2[i];
-    }
-    __syncthreads();
-  }
+  return !primary;
 }
 
 struct BigArgs {
@@ -232,14 +199,33 @@ struct BigArgs {
   int* retry_out;          // append list of nodes (phase 1 decide)
   int* nretry_out;
   int* big_index;          // node id -> index in `big` (for phase 2)
+  uint32_t* pv;            // classification: label << 27 | weight per entry slot of the big nodes
 };
 
-// Boundary scan of a sorted item: each thread owns 8 consecutive elements.
-// Values: classification items carry (label << 27 | weight) through the sort
-// (packed == true); otherwise the value is the entry index into elab/ew/eq.
+// Packed (label << 27 | weight) values of the big classification nodes' entries,
+// once per level instead of a label gather per try.
 template <int CW>
-__device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed, const int* elab,
-                             const int* ew, const long long* eq, int m, const LNode& nd,
+__global__ void __launch_bounds__(kBigBlock) k_big_pack(BigArgs b) {
+  const LevelArgs& a = b.L;
+  for (int ni = blockIdx.x; ni < b.nbig; ni += gridDim.x) {
+    const LNode nd = a.nodes[b.big[ni]];
+    const ProbDesc& P = a.probs[nd.prob];
+    if (P.task != 0) continue;
+    for (int i = threadIdx.x; i < nd.ecnt; i += kBigBlock) {
+      const long long e = nd.ebeg + i;
+      b.pv[e] = ((uint32_t)__ldg(P.lab + __ldg(a.rowsA + e)) << 27) |
+                (uint32_t)(a.wA ? __ldg(a.wA + e) : 1);
+    }
+  }
+}
+
+// Boundary scan of a sorted item: each thread owns `per` (1..8) consecutive
+// elements of every tile of 256 * per.  Classification items carry
+// (label << 27 | weight) through the sort (packed == true); regression items
+// carry the entry index into ew / eq.
+template <int CW>
+__device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed, const int* ew,
+                             const long long* eq, int m, int per, const LNode& nd,
                              const ProbDesc& P, const int* ncnt, const long long* H, long long prior,
                              unsigned long long* scan64, float* out_g, int* out_p, long long* out_nl,
                              long long* out_sl, unsigned long long (&outL)[CW]) {
@@ -247,7 +233,7 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
   const int ml = max(1, P.min_leaf);
   int Nt[2 * CW];
 #pragma unroll
-  for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
+  for (int c = 0; c < 2 * CW; ++c) Nt[c] = (packed && c < C) ? ncnt[c] : 0;
   float bg = -FLT_MAX;
   int bp = -1;
   long long bnl = 0, bsl = 0;
@@ -259,54 +245,54 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
     bL[j] = 0;
     carry[j] = 0;
   }
-  for (int base = 0; base < m; base += kBigTile) {
-    const int p0 = base + threadIdx.x * kBigPer;
-    uint32_t kk[kBigPer];
-    int lab[kBigPer], w[kBigPer];
-    long long q[kBigPer];
-#pragma unroll
-    for (int j = 0; j < kBigPer; ++j) {
-      const int p = p0 + j;
-      if (p < m) {
-        kk[j] = sk[p];
-        const uint32_t vv = sv[p];
-        if (packed) {
-          lab[j] = (int)(vv >> 27);
-          w[j] = (int)(vv & 0x7FFFFFFu);
-          q[j] = 0;
-        } else if (P.task == 0) {
-          const int e = (int)vv;
-          w[j] = ew ? ew[e] : 1;
-          lab[j] = elab[e];
-          q[j] = 0;
-        } else {
-          const int e = (int)vv;
-          w[j] = ew ? ew[e] : 1;
-          lab[j] = -1;
-          q[j] = eq[e];
-        }
-      } else {
-        kk[j] = 0xFFFFFFFFu;
-        w[j] = 0;
-        lab[j] = -1;
-        q[j] = 0;
-      }
-    }
+  for (int base = 0; base < m; base += kBigBlock * per) {
+    const int p0 = base + threadIdx.x * per;
     const uint32_t prevk0 = p0 > 0 && p0 - 1 < m ? sk[p0 - 1] : 0u;
-    // per-thread totals -> block exclusive scans
+    // per-thread totals (classification: from the packed values, which the
+    // scan below reads again, and a bit mask of the key boundaries;
+    // regression: keys, weights and targets kept in registers)
     long long tn = 0, ts = 0;
     unsigned long long tl[CW];
 #pragma unroll
     for (int c = 0; c < CW; ++c) tl[c] = 0;
+    uint32_t kk[kBigPer];
+    int w[kBigPer];
+    long long q[kBigPer];
+    unsigned bnd = 0;  // classification: bit j set when element j starts a new key
+    if (packed) {
+      uint32_t prev = prevk0;
 #pragma unroll
-    for (int j = 0; j < kBigPer; ++j) {
-      tn += w[j];
-      if (P.task == 0) {
+      for (int j = 0; j < kBigPer; ++j) {
+        const int p = p0 + j;
+        if (j < per && p < m) {
+          const uint32_t kj = sk[p];
+          const uint32_t vv = sv[p];
+          if (p > 0 && prev < kj) bnd |= 1u << j;
+          prev = kj;
+          const int lj = (int)(vv >> 27);
+          const int wj = (int)(vv & 0x7FFFFFFu);
+          tn += wj;
 #pragma unroll
-        for (int c = 0; c < CW; ++c)
-          tl[c] += (lab[j] == 2 * c ? (unsigned long long)w[j] : 0ull) |
-                   (lab[j] == 2 * c + 1 ? ((unsigned long long)w[j] << 32) : 0ull);
-      } else {
+          for (int c = 0; c < CW; ++c)
+            tl[c] += (lj == 2 * c ? (unsigned long long)wj : 0ull) |
+                     (lj == 2 * c + 1 ? ((unsigned long long)wj << 32) : 0ull);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kBigPer; ++j) {
+        const int p = p0 + j;
+        if (j < per && p < m) {
+          kk[j] = sk[p];
+          const int e = (int)sv[p];
+          w[j] = ew ? ew[e] : 1;
+          q[j] = eq[e];
+        } else {
+          kk[j] = 0xFFFFFFFFu;
+          w[j] = 0;
+          q[j] = 0;
+        }
+        tn += w[j];
         ts += q[j] * (long long)w[j];
       }
     }
@@ -315,13 +301,13 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
     unsigned long long sv_[CW + 1], tot[CW + 1];
     sv_[0] = (unsigned long long)tn;
 #pragma unroll
-    for (int c = 0; c < CW; ++c) sv_[1 + c] = P.task == 0 ? tl[c] : (c == 0 ? (unsigned long long)ts : 0ull);
+    for (int c = 0; c < CW; ++c) sv_[1 + c] = packed ? tl[c] : (c == 0 ? (unsigned long long)ts : 0ull);
     block_excl_scan_n<kBigBlock, CW + 1>(sv_, tot, scan64);
     long long run_n = carry_n + (long long)sv_[0];
     carry_n += (long long)tot[0];
     long long run_s = 0;
     unsigned long long runL[CW];
-    if (P.task == 0) {
+    if (packed) {
 #pragma unroll
       for (int c = 0; c < CW; ++c) {
         runL[c] = carry[c] + sv_[1 + c];
@@ -335,21 +321,19 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
     }
     uint32_t prevk = prevk0;
     if (packed) {
-      // classification: a rolled loop that re-reads each (key, label|weight)
-      // pair; the 2C-term entropy gain is the bulk of the kernel's code and
+      // classification: a rolled loop that re-reads each label|weight value;
+      // the 2C-term entropy gain is the bulk of the kernel's code and
       // unrolled eight times it overflows the instruction cache
 #pragma unroll 1
-      for (int j = 0; j < kBigPer; ++j) {
+      for (int j = 0; j < per; ++j) {
         const int p = p0 + j;
-        uint32_t kj = 0xFFFFFFFFu;
         int wj = 0, labj = -1;
         if (p < m) {
-          kj = sk[p];
           const uint32_t vv = sv[p];
           labj = (int)(vv >> 27);
           wj = (int)(vv & 0x7FFFFFFu);
         }
-        if (p < m && p > 0 && prevk < kj) {
+        if ((bnd >> j) & 1u) {
           const long long nr = (long long)nd.n - run_n;
           if (run_n >= ml && nr >= ml) {
             const float g = entropy_gain_u<2 * CW>(
@@ -368,7 +352,6 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
             }
           }
         }
-        prevk = kj;
         run_n += wj;
 #pragma unroll
         for (int c = 0; c < CW; ++c)
@@ -376,45 +359,25 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
                      (labj == 2 * c + 1 ? ((unsigned long long)wj << 32) : 0ull);
       }
     } else {
-      // entry-indexed values (regression, or unpacked labels): the gathered
-      // weights and targets stay in registers, all loads already in flight
+      // regression: the gathered weights and targets stay in registers
 #pragma unroll
       for (int j = 0; j < kBigPer; ++j) {
         const int p = p0 + j;
-        if (p < m && p > 0 && prevk < kk[j]) {
+        if (j < per && p < m && p > 0 && prevk < kk[j]) {
           const long long nr = (long long)nd.n - run_n;
           if (run_n >= ml && nr >= ml) {
-            float g;
-            if (P.task == 0)
-              g = entropy_gain_u<2 * CW>(
-                  H, prior, C, run_n, nr,
-                  [&](int c) {
-                    return (long long)((c & 1) ? (runL[c >> 1] >> 32)
-                                               : (runL[c >> 1] & 0xFFFFFFFFull));
-                  },
-                  [&](int c) { return (long long)Nt[c]; });
-            else
-              g = variance_gain(run_n, run_s, nr, nd.sum - run_s, P.S);
+            const float g = variance_gain(run_n, run_s, nr, nd.sum - run_s, P.S);
             if (bp < 0 || g > bg) {
               bg = g;
               bp = p;
               bnl = run_n;
               bsl = run_s;
-#pragma unroll
-              for (int c = 0; c < CW; ++c) bL[c] = runL[c];
             }
           }
         }
         prevk = kk[j];
         run_n += w[j];
-        if (P.task == 0) {
-#pragma unroll
-          for (int c = 0; c < CW; ++c)
-            runL[c] += (lab[j] == 2 * c ? (unsigned long long)w[j] : 0ull) |
-                       (lab[j] == 2 * c + 1 ? ((unsigned long long)w[j] << 32) : 0ull);
-        } else {
-          run_s += q[j] * (long long)w[j];
-        }
+        run_s += q[j] * (long long)w[j];
       }
     }
   }
@@ -457,9 +420,16 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     if (threadIdx.x == 0 && P.task == 0)
       s_prior = entropy_prior(a.H, nd.n, P.C, [&](int c) { return (long long)ncnt[c]; });
     // keys (and, for classification, the packed label | weight values) with
-    // eight gathers in flight per thread
+    // eight gathers in flight per thread; the keys' OR / AND and the digit
+    // histograms of their significant bytes on the way
     const bool packed = P.task == 0;
     const int* wts = a.wA ? a.wA + nd.ebeg : nullptr;
+    const uint32_t* pv = b.pv ? b.pv + nd.ebeg : nullptr;
+    const uint32_t* rk = P.rank ? P.rank + (long long)f * P.N : nullptr;
+    const int nbytes = rk ? (32 - __clz(max(1ll, P.N - 1)) + 7) >> 3 : 4;
+    for (int i = threadIdx.x; i < 4 * 256; i += kBigBlock) (&S.dh[0][0])[i] = 0;
+    __syncthreads();
+    unsigned o = 0, an = 0xFFFFFFFFu;
     for (int base = 0; base < m; base += kBigTile) {
       int rr[kBigPer];
 #pragma unroll
@@ -470,19 +440,44 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
 #pragma unroll
       for (int j = 0; j < kBigPer; ++j) {
         const int i = base + j * kBigBlock + threadIdx.x;
-        if (i < m) {
-          k1[i] = P.rank ? __ldg(P.rank + (long long)f * P.N + rr[j])
-                         : orderable(__ldg(xf + rr[j]));
-          v1[i] = packed ? ((uint32_t)__ldg(P.lab + rr[j]) << 27) |
-                               (uint32_t)(wts ? __ldg(wts + i) : 1)
-                         : (uint32_t)i;
+        const bool act = i < m;
+        uint32_t k = 0;
+        if (act) {
+          k = rk ? __ldg(rk + rr[j]) : orderable(__ldg(xf + rr[j]));
+          k1[i] = k;
+          v1[i] = packed ? __ldg(pv + i) : (uint32_t)i;
+          o |= k;
+          an &= k;
         }
+        for (int d = 0; d < nbytes; ++d) hist_add_round(S.dh[d], (k >> (8 * d)) & 255u, act);
       }
     }
+#pragma unroll
+    for (int sh = 16; sh > 0; sh >>= 1) {
+      o |= __shfl_xor_sync(kFull, o, sh);
+      an &= __shfl_xor_sync(kFull, an, sh);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      S.red[2 * (threadIdx.x >> 5)] = o;
+      S.red[2 * (threadIdx.x >> 5) + 1] = an;
+    }
     __syncthreads();
-    big_sort(k1, v1, k2, v2, m, S);
-    // regression: per-entry targets in the free second buffer
-    long long* eq = (long long*)k2;  // k2, v2 contiguous: 8 bytes per entry
+    unsigned diff;
+    {
+      unsigned oo = 0, aa = 0xFFFFFFFFu;
+#pragma unroll
+      for (int w = 0; w < kBigWarps; ++w) {
+        oo |= S.red[2 * w];
+        aa &= S.red[2 * w + 1];
+      }
+      diff = oo ^ aa;
+    }
+    // S.red is written again only after the sort's and the scan's barriers
+    const bool in2 = big_sort(k1, v1, k2, v2, m, diff, S);
+    const uint32_t* sk = in2 ? k2 : k1;
+    const uint32_t* sv = in2 ? v2 : v1;
+    // regression: per-entry targets in the free pair buffer (8 bytes per entry)
+    long long* eq = (long long*)(in2 ? k1 : k2);
     if (!packed) {
       for (int i = threadIdx.x; i < m; i += kBigBlock) eq[i] = __ldg(P.q + __ldg(rows + i));
       __syncthreads();
@@ -491,7 +486,7 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     int p;
     long long nl, sl;
     unsigned long long L[CW];
-    big_boundary<CW>(k1, v1, packed, nullptr, wts, eq, m, nd, P, ncnt, a.H, s_prior, S.scan64, &g,
+    big_boundary<CW>(sk, sv, packed, wts, eq, m, kBigPer, nd, P, ncnt, a.H, s_prior, S.scan64, &g,
                      &p, &nl, &sl, L);
     const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
     if (bp >= 0 && p == bp) {
@@ -501,8 +496,8 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
       c.f = f;
       // the values on both sides of the boundary (-0 reads back as +0, which
       // gives the same threshold)
-      const float xa = packed ? key_value(P, f, k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
-      const float xb = packed ? key_value(P, f, k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
+      const float xa = packed ? key_value(P, f, sk[bp - 1]) : __ldg(xf + __ldg(rows + sv[bp - 1]));
+      const float xb = packed ? key_value(P, f, sk[bp]) : __ldg(xf + __ldg(rows + sv[bp]));
       c.thr = midpoint_threshold(xa, xb);
       c.nl_e = bp;
       c.nl = (int)nl;
@@ -608,10 +603,16 @@ __global__ void __launch_bounds__(kBigBlock) k_rf_big_decide(BigArgs b) {
   }
 }
 
-// RF node of 257 .. SMEM_CAP entries in one CTA: keys and values sorted in
-// shared memory, then the same 8-per-thread boundary scan as the large path.
+// RF node of 257 .. a.smem_cap (<= SMEM_CAP) entries in one CTA.  The node's
+// row ids and packed (label << 27 | weight) values are read into shared memory
+// once per node; each try gathers the feature's keys (reducing their varying
+// bits on the way), sorts the (key, value) pairs in shared memory and scans
+// the boundaries with ceil(m / 256) consecutive elements per thread.
+// Dynamic shared memory, 24 bytes per entry of a.smem_cap:
+//   classification: k1 v1 k2 v2 (sort buffers), row ids, packed values;
+//   regression:     k1 v1 k2 v2, fixed-point targets (8 bytes).
 template <int CW, int SMEM_CAP>
-__global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
+__global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_smem(LevelArgs a) {
   __shared__ SortSmem<kBigBlock> SS;
   __shared__ unsigned red[2 * kBigWarps];
   __shared__ unsigned long long scan64[kBigWarps * (CW + 1)];
@@ -623,23 +624,35 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
   __shared__ int s_scan[kBigWarps];
   __shared__ int s_next;
   extern __shared__ __align__(16) unsigned char dsm[];
+  const int cap = a.smem_cap;
   uint32_t* k1 = (uint32_t*)dsm;
-  uint32_t* v1 = k1 + SMEM_CAP;
-  uint32_t* k2 = k1 + 2 * SMEM_CAP;
-  uint32_t* v2 = k1 + 3 * SMEM_CAP;
-  long long* q_e = (long long*)(k1 + 4 * SMEM_CAP);
+  uint32_t* v1 = k1 + cap;
+  uint32_t* k2 = k1 + 2 * cap;
+  uint32_t* v2 = k1 + 3 * cap;
+  int* s_rows = (int*)(k1 + 4 * cap);
+  uint32_t* s_pv = k1 + 5 * cap;
+  long long* q_e = (long long*)(k1 + 4 * cap);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int wi = blockIdx.x; wi < a.nwork; wi += gridDim.x) {
     const int node = a.work[wi];
     const LNode nd = a.nodes[node];
     const ProbDesc& P = a.probs[nd.prob];
     const int C = P.C;
     const int m = nd.ecnt;
+    const int per = min(kBigPer, (m + kBigBlock - 1) / kBigBlock);
     const int* rows = a.rowsA + nd.ebeg;
     const int* wts = a.wA ? a.wA + nd.ebeg : nullptr;
     const int* ncnt = a.cnt + (long long)node * a.Cmax;
     const bool packed = P.task == 0;
-    if (!packed)
+    if (packed) {
+      for (int i = threadIdx.x; i < m; i += kBigBlock) {
+        const int row = __ldg(rows + i);
+        s_rows[i] = row;
+        s_pv[i] = ((uint32_t)__ldg(P.lab + row) << 27) | (uint32_t)(wts ? __ldg(wts + i) : 1);
+      }
+    } else {
       for (int i = threadIdx.x; i < m; i += kBigBlock) q_e[i] = __ldg(P.q + __ldg(rows + i));
+    }
     if (threadIdx.x == 0 && packed)
       s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     __syncthreads();
@@ -647,28 +660,65 @@ __global__ void __launch_bounds__(kBigBlock, 2) k_rf_smem(LevelArgs a) {
     while (true) {
       const int f = feature_of_try(P, nd, t);
       const float* xf = P.X + (long long)f * P.N;
-      for (int i = threadIdx.x; i < m; i += kBigBlock) {
-        const int row = __ldg(rows + i);
-        k1[i] = P.rank ? __ldg(P.rank + (long long)f * P.N + row) : orderable(__ldg(xf + row));
-        v1[i] = packed ? ((uint32_t)__ldg(P.lab + row) << 27) | (uint32_t)(wts ? __ldg(wts + i) : 1)
-                       : (uint32_t)i;
+      const uint32_t* rk = P.rank ? P.rank + (long long)f * P.N : nullptr;
+      unsigned o = 0, an = 0xFFFFFFFFu;
+      if (packed) {
+        for (int i = threadIdx.x; i < m; i += kBigBlock) {
+          const int row = s_rows[i];
+          const uint32_t k = rk ? __ldg(rk + row) : orderable(__ldg(xf + row));
+          k1[i] = k;
+          v1[i] = s_pv[i];
+          o |= k;
+          an &= k;
+        }
+      } else {
+        for (int i = threadIdx.x; i < m; i += kBigBlock) {
+          const int row = __ldg(rows + i);
+          const uint32_t k = rk ? __ldg(rk + row) : orderable(__ldg(xf + row));
+          k1[i] = k;
+          v1[i] = (uint32_t)i;
+          o |= k;
+          an &= k;
+        }
+      }
+#pragma unroll
+      for (int sh = 16; sh > 0; sh >>= 1) {
+        o |= __shfl_xor_sync(kFull, o, sh);
+        an &= __shfl_xor_sync(kFull, an, sh);
+      }
+      if (lane == 0) {
+        red[2 * warp] = o;
+        red[2 * warp + 1] = an;
       }
       __syncthreads();
-      cta_radix_sort<kBigBlock>(k1, v1, k2, v2, m, SS, red);
+      unsigned diff;
+      {
+        unsigned oo = 0, aa = 0xFFFFFFFFu;
+#pragma unroll
+        for (int w = 0; w < kBigWarps; ++w) {
+          oo |= red[2 * w];
+          aa &= red[2 * w + 1];
+        }
+        diff = oo ^ aa;
+      }
+      // red is written again only after the sort's and the scan's barriers
+      const bool in2 = cta_radix_sort_diff<kBigBlock>(k1, v1, k2, v2, m, diff, SS);
+      const uint32_t* sk = in2 ? k2 : k1;
+      const uint32_t* sv = in2 ? v2 : v1;
       float g;
       int p;
       long long nl, sl;
       unsigned long long L[CW];
-      big_boundary<CW>(k1, v1, packed, nullptr, wts, q_e, m, nd, P, ncnt, a.H, s_prior, scan64,
-                       &g, &p, &nl, &sl, L);
+      big_boundary<CW>(sk, sv, packed, wts, q_e, m, per, nd, P, ncnt, a.H, s_prior,
+                       scan64, &g, &p, &nl, &sl, L);
       const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
       if (bp >= 0 && p == bp) {
         Cand c;
         c.valid = 1;
         c.gain = g;
         c.f = f;
-        const float xa = packed ? key_value(P, f, k1[bp - 1]) : __ldg(xf + __ldg(rows + v1[bp - 1]));
-        const float xb = packed ? key_value(P, f, k1[bp]) : __ldg(xf + __ldg(rows + v1[bp]));
+        const float xa = packed ? key_value(P, f, sk[bp - 1]) : __ldg(xf + __ldg(rows + sv[bp - 1]));
+        const float xb = packed ? key_value(P, f, sk[bp]) : __ldg(xf + __ldg(rows + sv[bp]));
         c.thr = midpoint_threshold(xa, xb);
         c.nl_e = bp;
         c.nl = (int)nl;

@@ -47,8 +47,10 @@ int quant_scale_from_max(float maxabs, long long n);
 
 dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s);
 
-// Largest RF node (entries) the shared-memory search kernel can hold.
+// Largest RF node (entries) the shared-memory search kernel can hold, and the
+// default: with buffers of 2048 entries (48 KB) three CTAs fit an SM.
 constexpr int kSearchSmemCap = 4096;
+constexpr int kDefaultSmemCap = 2048;
 
 // Scheduling of a fit (tuning.cu): RF nodes of up to warp_max entries (64, 128
 // or 256) are searched by a warp, up to smem_cap by a CTA in shared memory,

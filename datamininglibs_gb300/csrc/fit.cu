@@ -452,6 +452,10 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     }
     uint32_t* big_slot =
         slot_stride > 0 ? (uint32_t*)alloc(sizeof(uint32_t) * 4 * slot_stride * big_grid) : nullptr;
+    bool any_cls = false;
+    for (auto& P : hp) any_cls = any_cls || P.task == 0;
+    uint32_t* big_pv =
+        slot_stride > 0 && any_cls ? (uint32_t*)alloc(sizeof(uint32_t) * total_slots) : nullptr;
     int* d_nretry = (int*)alloc(sizeof(int));
     ProbDesc* d_probs = (ProbDesc*)alloc(sizeof(ProbDesc) * nprob);
     DML_CK(cudaMemcpyAsync(d_probs, hp.data(), sizeof(ProbDesc) * nprob, cudaMemcpyHostToDevice, s));
@@ -548,6 +552,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       a.scratch_half = total_slots;
       a.H = H;
       a.stats = d_stats;
+      a.smem_cap = tune.smem_cap;
       int qc[kNumQ];
       std::memcpy(qc, h_sum->qcount, sizeof(qc));
       DML_CK(cudaEventRecord(es0, s));
@@ -578,6 +583,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           b.retry_out = big_retry.p;
           b.nretry_out = d_nretry;
           b.big_index = big_index.p;
+          b.pv = big_pv;
           DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
           b.L.stats = d_stats + 4 + 4 * q;
           DML_CK(cudaEventRecord(qev[q][0], s));
@@ -588,8 +594,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
             DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
             launch_big(CW, b, 1, big_grid, std::min(b.nbig, 65535), max_mand, s);
             launch_big(CW, b, 2, big_grid, std::min(b.nbig, 65535), std::max(1, max_opt), s);
-            st.launches += 4;
-            queue_launches[q] += 4;
+            st.launches += big_pv ? 5 : 4;
+            queue_launches[q] += big_pv ? 5 : 4;
             if (plain) DML_CK(cudaStreamSynchronize(s));
           }
           DML_CK(cudaEventRecord(qev[q][1], s));
@@ -1139,6 +1145,7 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
       a.scratch_half = 0;
       a.H = H;
       a.stats = d_stats;
+      a.smem_cap = kSmemCap;
       for (int q = 0; q < kNumQ; ++q) {
         if (qc[q] <= 0) continue;
         if (q == kQRfBig) {

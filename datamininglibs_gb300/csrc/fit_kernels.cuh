@@ -265,6 +265,7 @@ struct LevelArgs {
   long long scratch_half;
   const long long* H;   // n*ln(n) table, fixed point 2^-28
   long long* stats;     // [2] += tries evaluated x node entries, [3] += node entries
+  int smem_cap;         // entries per node of the shared-memory RF search's buffers
 };
 
 // ================================================================== ERT (CTA)
@@ -535,6 +536,24 @@ __device__ void radix_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* k
     __syncwarp();
   }
   __syncthreads();
+}
+
+// Sorts pairs whose varying key bits are `diff` (OR ^ AND of all keys, which
+// the caller reduced while writing them).  Passes whose digit is constant are
+// skipped; returns true when the sorted pairs are in k2/v2, false when in k/v.
+template <int BLOCK>
+__device__ bool cta_radix_sort_diff(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2, int m,
+                                    unsigned diff, SortSmem<BLOCK>& S) {
+  bool in_primary = true;
+  for (int shift = 0; shift < 32; shift += 8) {
+    if (((diff >> shift) & 255u) == 0) continue;
+    if (in_primary)
+      radix_pass<BLOCK>(k, v, k2, v2, m, shift, S);
+    else
+      radix_pass<BLOCK>(k2, v2, k, v, m, shift, S);
+    in_primary = !in_primary;
+  }
+  return !in_primary;
 }
 
 // Sorts pairs in place (result back in k/v).  Passes whose digit is constant

@@ -49,7 +49,7 @@ void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s) {
     k_ert_cta<kBlock><<<std::min(count, 1 << 20), kBlock, 0, s>>>(b);
   } else {
     set_smem_attrs<CW>();
-    k_rf_smem<CW, kSmemCap><<<std::min(count, 1 << 20), kBlock, (size_t)kSmemCap * 24, s>>>(b);
+    k_rf_smem<CW, kSmemCap><<<std::min(count, 1 << 20), kBlock, (size_t)b.smem_cap * 24, s>>>(b);
   }
   DML_CK(cudaGetLastError());
 }
@@ -58,6 +58,7 @@ template <int CW>
 void launch_big_cw(BigArgs b, int phase, int grid, int decide_grid, int tries, cudaStream_t s) {
   b.phase = phase;
   b.tries_per_node = tries;
+  if (phase == 1 && b.pv) k_big_pack<CW><<<decide_grid, kBigBlock, 0, s>>>(b);
   k_rf_big_items<CW><<<grid, kBigBlock, 0, s>>>(b);
   k_rf_big_decide<CW><<<decide_grid, kBigBlock, 0, s>>>(b);
   DML_CK(cudaGetLastError());

@@ -88,7 +88,7 @@ bool valid_tuning(const Tuning& t) {
          t.smem_cap <= kSearchSmemCap && t.big_ctas >= 1 && t.big_ctas <= 3;
 }
 
-Tuning default_tuning(int CW) { return Tuning{256, kSearchSmemCap, big_ctas_per_sm(CW)}; }
+Tuning default_tuning(int CW) { return Tuning{256, kDefaultSmemCap, big_ctas_per_sm(CW)}; }
 
 // The tuning of a fit: the forced candidate, the stored tuning of the largest
 // problem's bucket, or the defaults.
