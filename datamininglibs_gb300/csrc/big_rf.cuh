@@ -234,8 +234,10 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
   int Nt[2 * CW];
 #pragma unroll
   for (int c = 0; c < 2 * CW; ++c) Nt[c] = (packed && c < C) ? ncnt[c] : 0;
-  float bg = -FLT_MAX;
+  float bg = -FLT_MAX;  // regression
   int bp = -1;
+  NumBest nb;  // classification
+  nb.init();
   long long bnl = 0, bsl = 0;
   unsigned long long bL[CW];
   unsigned long long carry[CW];
@@ -321,35 +323,30 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
     }
     uint32_t prevk = prevk0;
     if (packed) {
-      // classification: a rolled loop that re-reads each label|weight value;
-      // the 2C-term entropy gain is the bulk of the kernel's code and
-      // unrolled eight times it overflows the instruction cache
+      // classification: a rolled loop that re-reads each label|weight value
+      // (the class terms unrolled eight times overflow the instruction cache);
+      // boundaries are compared on their exact gain numerators P - Q
 #pragma unroll 1
       for (int j = 0; j < per; ++j) {
         const int p = p0 + j;
-        int wj = 0, labj = -1;
+        int wj = 0, labj = 0;
         if (p < m) {
           const uint32_t vv = sv[p];
           labj = (int)(vv >> 27);
           wj = (int)(vv & 0x7FFFFFFu);
         }
-        if ((bnd >> j) & 1u) {
-          const long long nr = (long long)nd.n - run_n;
-          if (run_n >= ml && nr >= ml) {
-            const float g = entropy_gain_u<2 * CW>(
-                H, prior, C, run_n, nr,
-                [&](int c) {
-                  return (long long)((c & 1) ? (runL[c >> 1] >> 32)
-                                             : (runL[c >> 1] & 0xFFFFFFFFull));
-                },
-                [&](int c) { return (long long)Nt[c]; });
-            if (bp < 0 || g > bg) {
-              bg = g;
-              bp = p;
-              bnl = run_n;
+        const long long nr = (long long)nd.n - run_n;
+        if (((bnd >> j) & 1u) && run_n >= ml && nr >= ml) {
+          const long long Q = entropy_q_u<2 * CW>(
+              H, C, run_n, nr,
+              [&](int c) {
+                return (long long)((c & 1) ? (runL[c >> 1] >> 32) : (runL[c >> 1] & 0xFFFFFFFFull));
+              },
+              [&](int c) { return (long long)Nt[c]; });
+          if (nb.offer(prior - Q, p, nd.n)) {
+            bnl = run_n;
 #pragma unroll
-              for (int c = 0; c < CW; ++c) bL[c] = runL[c];
-            }
+            for (int c = 0; c < CW; ++c) bL[c] = runL[c];
           }
         }
         run_n += wj;
@@ -381,8 +378,8 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
       }
     }
   }
-  *out_g = bg;
-  *out_p = bp;
+  *out_g = packed ? nb.gain(nd.n) : bg;
+  *out_p = packed ? nb.p : bp;
   *out_nl = bnl;
   *out_sl = bsl;
 #pragma unroll

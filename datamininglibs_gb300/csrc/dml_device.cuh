@@ -176,12 +176,12 @@ __device__ __forceinline__ float entropy_gain(const long long* H, long long P, i
   return gain_from_numerator(P - Q, nL + nR);
 }
 
-// The same with the class loop unrolled to a compile-time bound CMAX >= C, so
-// that per-class counts held in registers are read without index arithmetic.
+// Q of a split with the class loop unrolled to a compile-time bound CMAX >= C,
+// so that per-class counts held in registers are read without index
+// arithmetic.  The split's gain numerator is P - Q.
 template <int CMAX, class LeftFn, class TotFn>
-__device__ __forceinline__ float entropy_gain_u(const long long* H, long long P, int C,
-                                                long long nL, long long nR, LeftFn L,
-                                                TotFn Ntot) {
+__device__ __forceinline__ long long entropy_q_u(const long long* H, int C, long long nL,
+                                                 long long nR, LeftFn L, TotFn Ntot) {
   long long Q = __ldg(H + nL) + __ldg(H + nR);
 #pragma unroll
   for (int c = 0; c < CMAX; ++c)
@@ -189,8 +189,70 @@ __device__ __forceinline__ float entropy_gain_u(const long long* H, long long P,
       const long long l = L(c);
       Q -= __ldg(H + l) + __ldg(H + (Ntot(c) - l));
     }
-  return gain_from_numerator(P - Q, nL + nR);
+  return Q;
 }
+
+template <int CMAX, class LeftFn, class TotFn>
+__device__ __forceinline__ float entropy_gain_u(const long long* H, long long P, int C,
+                                                long long nL, long long nR, LeftFn L,
+                                                TotFn Ntot) {
+  return gain_from_numerator(P - entropy_q_u<CMAX>(H, C, nL, nR, L, Ntot), nL + nR);
+}
+
+// Change of Q when one entry of class c and weight w moves from the right side
+// (nR rows, Rc of class c) to the left (nL rows, Lc of class c).  Integer
+// terms, so Q kept this way equals Q recomputed.
+__device__ __forceinline__ long long entropy_q_move(const long long* H, long long nL,
+                                                    long long nR, long long Lc, long long Rc,
+                                                    long long w) {
+  return (__ldg(H + nL + w) - __ldg(H + nL)) + (__ldg(H + nR - w) - __ldg(H + nR)) -
+         (__ldg(H + Lc + w) - __ldg(H + Lc)) - (__ldg(H + Rc - w) - __ldg(H + Rc));
+}
+
+// For numerators d > dtop of one node: false when gain_from_numerator(d) is
+// certainly above gain_from_numerator(dtop).  The int64 -> float conversion
+// and the two rounded operations that follow move a value by at most 2^-24
+// relative each, so numerators more than 2^-21 apart (relative to the larger
+// magnitude) give different gains; only closer ones need their gains compared.
+__device__ __forceinline__ bool gain_may_tie(long long d, long long dtop) {
+  const unsigned long long ad = d < 0 ? 0ull - (unsigned long long)d : (unsigned long long)d;
+  const unsigned long long at =
+      dtop < 0 ? 0ull - (unsigned long long)dtop : (unsigned long long)dtop;
+  const unsigned long long mx = ad > at ? ad : at;
+  return (unsigned long long)(d - dtop) <= (mx >> 21);
+}
+
+// Best boundary of one thread that offers its positions in increasing order:
+// the first position of the highest gain, found on exact gain numerators of
+// one node (n rows).  The gain is monotone in the numerator, so a numerator
+// that does not exceed the highest one seen cannot win; a float gain is
+// computed only when two numerators are close enough to round to the same one.
+// The best gain is always the gain of `top`.
+struct NumBest {
+  long long top;
+  int p;  // -1 before the first offer
+  __device__ __forceinline__ void init() {
+    p = -1;
+    top = 0;
+  }
+  // True when `pos` becomes the best position.
+  __device__ __forceinline__ bool offer(long long d, int pos, long long n) {
+    if (p < 0) {
+      p = pos;
+      top = d;
+      return true;
+    }
+    if (d <= top) return false;
+    const bool take =
+        !gain_may_tie(d, top) || gain_from_numerator(d, n) > gain_from_numerator(top, n);
+    top = d;
+    if (take) p = pos;
+    return take;
+  }
+  __device__ __forceinline__ float gain(long long n) const {
+    return p < 0 ? -FLT_MAX : gain_from_numerator(top, n);
+  }
+};
 
 __device__ __forceinline__ float variance_gain(long long nL, long long SL, long long nR,
                                                long long SR, int S) {

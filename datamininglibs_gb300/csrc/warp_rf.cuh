@@ -61,6 +61,17 @@ __device__ __forceinline__ long long packed_get(const unsigned long long (&L)[CW
   return (long long)((c & 1) ? (x >> 32) : (x & 0xFFFFFFFFull));
 }
 
+// Nt[c] for a class index known only at run time (a select chain over the
+// registers instead of a local-memory array).
+template <int CW>
+__device__ __forceinline__ int Nt_of(const int (&Nt)[2 * CW], int c) {
+  int x = Nt[0];
+#pragma unroll
+  for (int j = 1; j < 2 * CW; ++j)
+    if (c == j) x = Nt[j];
+  return x;
+}
+
 // Warps per block: 8, or 4 for 512-entry nodes (shared memory per warp).
 template <int E>
 constexpr int warp_rf_wpb() {
@@ -75,7 +86,9 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
   __shared__ int s_w[WPB][M];
   __shared__ int s_lab[WPB][M];
   __shared__ long long s_q[WPB][M];
-  __shared__ unsigned long long s_key[WPB][M];  // sorted (key, entry) of the current try
+  // sorted (key, entry) of the current try; sorted position p at p + p / E, so
+  // that lane l's E consecutive positions are read without bank conflicts
+  __shared__ unsigned long long s_key[WPB][M + 32];
   const int lane = threadIdx.x & 31;
   const int wb = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -129,75 +142,112 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
       }
       warp_bitonic_sort<E>(key);
 #pragma unroll
-      for (int r = 0; r < E; ++r) s_key[wb][r * 32 + lane] = key[r];
+      for (int r = 0; r < E; ++r) s_key[wb][r * 32 + lane + (r * 32 + lane) / E] = key[r];
       __syncwarp();
-      // boundary scan, 32 sorted elements per round (a rolled loop: the
-      // per-round class scans and gains are the bulk of the kernel's code)
-      unsigned long long carryL[CW], L[CW], myL[CW];
+      // boundary scan: lane l owns sorted positions l*E .. l*E+E-1.  One warp
+      // scan of the lanes' row counts and packed class counts (or target
+      // sums), then each lane walks its positions (rolled loops re-reading
+      // shared memory: the class terms are the bulk of the kernel's code).
+      const int p0 = lane * E;
+      const unsigned long long* sk = &s_key[wb][p0 + lane];
+      long long tn = 0, ts = 0;
+      unsigned long long tl[CW];
 #pragma unroll
-      for (int j = 0; j < CW; ++j) {
-        carryL[j] = 0;
-        myL[j] = 0;
-      }
-      long long carry_n = 0, carry_s = 0, my_nl = 0, my_sl = 0;
-      uint32_t lastk = 0;
-      float bg = -FLT_MAX;
-      int bp = -1;
+      for (int c = 0; c < CW; ++c) tl[c] = 0;
+      unsigned bnd = 0;  // bit j: position p0 + j starts a new key
+      uint32_t prevk =
+          p0 > 0 ? (uint32_t)(s_key[wb][p0 - 1 + (p0 - 1) / E] >> 32) : 0u;
 #pragma unroll 1
-      for (int r = 0; r < E; ++r) {
-        const unsigned long long kv = s_key[wb][r * 32 + lane];
-        const bool ok = kv != ~0ull;
+      for (int j = 0; j < E; ++j) {
+        const unsigned long long kv = sk[j];
+        if (kv == ~0ull) break;
         const int e = (int)(kv & 0xFFFFFFFFull);
         const uint32_t kk = (uint32_t)(kv >> 32);
-        const int pos = r * 32 + lane;
-        const int w = ok ? s_w[wb][e] : 0;
-        long long nl, sl = 0;
-        {
-          long long ex = warp_excl_scan<long long>(w);
-          nl = carry_n + ex;
-          carry_n += __shfl_sync(kFull, ex + w, 31);
-        }
+        if (p0 + j > 0 && prevk < kk) bnd |= 1u << j;
+        prevk = kk;
+        const int w = s_w[wb][e];
+        tn += w;
         if (P.task == 0) {
-          const int k = ok ? s_lab[wb][e] : -1;
+          const int k = s_lab[wb][e];
 #pragma unroll
-          for (int j = 0; j < CW; ++j) {
-            unsigned long long v = (k == 2 * j ? (unsigned long long)w : 0ull) |
-                                   (k == 2 * j + 1 ? ((unsigned long long)w << 32) : 0ull);
-            unsigned long long ex = warp_excl_scan<unsigned long long>(v);
-            L[j] = carryL[j] + ex;
-            carryL[j] += __shfl_sync(kFull, ex + v, 31);
-          }
+          for (int c = 0; c < CW; ++c)
+            tl[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
+                     (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
         } else {
-          const long long qw = ok ? s_q[wb][e] * (long long)w : 0;
-          long long ex = warp_excl_scan<long long>(qw);
-          sl = carry_s + ex;
-          carry_s += __shfl_sync(kFull, ex + qw, 31);
+          ts += s_q[wb][e] * (long long)w;
         }
-        uint32_t prevk = __shfl_up_sync(kFull, kk, 1);
-        if (lane == 0) prevk = lastk;
-        lastk = __shfl_sync(kFull, kk, 31);
-        const long long nr = (long long)nd.n - nl;
-        const bool bnd = ok && pos > 0 && prevk < kk && nl >= ml && nr >= ml;
-        if (bnd) {
-          float g;
-          if (P.task == 0)
-            g = entropy_gain_u<2 * CW>(
-                a.H, prior, C, nl, nr,
-                [&](int c) {
-                  return (long long)((c & 1) ? (L[c >> 1] >> 32) : (L[c >> 1] & 0xFFFFFFFFull));
-                },
-                [&](int c) { return (long long)Nt[c]; });
-          else
-            g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
-          if (bp < 0 || g > bg) {
-            bg = g;
-            bp = pos;
-            my_nl = nl;
-            my_sl = sl;
+      }
+      long long nl = warp_excl_scan<long long>(tn);
+      long long sl = 0;
+      unsigned long long L[CW];
+      if (P.task == 0) {
 #pragma unroll
-            for (int j = 0; j < CW; ++j) myL[j] = L[j];
+        for (int c = 0; c < CW; ++c) L[c] = warp_excl_scan<unsigned long long>(tl[c]);
+      } else {
+        sl = warp_excl_scan<long long>(ts);
+#pragma unroll
+        for (int c = 0; c < CW; ++c) L[c] = 0;
+      }
+      unsigned long long myL[CW];
+#pragma unroll
+      for (int c = 0; c < CW; ++c) myL[c] = 0;
+      long long my_nl = 0, my_sl = 0;
+      float bg = -FLT_MAX;
+      int bp = -1;
+      NumBest nb;
+      nb.init();
+      long long Q = 0;
+      bool haveQ = false;
+#pragma unroll 1
+      for (int j = 0; j < E && bnd >> j; ++j) {
+        const unsigned long long kv = sk[j];
+        const int e = (int)(kv & 0xFFFFFFFFull);
+        const int w = s_w[wb][e];
+        const long long nr = (long long)nd.n - nl;
+        const bool at = ((bnd >> j) & 1u) && nl >= ml && nr >= ml;
+        if (P.task == 0) {
+          const int k = s_lab[wb][e];
+          if (at) {
+            if (!haveQ) {
+              Q = entropy_q_u<2 * CW>(
+                  a.H, C, nl, nr,
+                  [&](int c) {
+                    return (long long)((c & 1) ? (L[c >> 1] >> 32) : (L[c >> 1] & 0xFFFFFFFFull));
+                  },
+                  [&](int c) { return (long long)Nt[c]; });
+              haveQ = true;
+            }
+            if (nb.offer(prior - Q, p0 + j, nd.n)) {
+              my_nl = nl;
+#pragma unroll
+              for (int c = 0; c < CW; ++c) myL[c] = L[c];
+            }
           }
+          if (haveQ && (bnd >> (j + 1)) != 0u) {
+            const long long lc = packed_get<CW>(L, k);
+            Q += entropy_q_move(a.H, nl, nr, lc, (long long)Nt_of<CW>(Nt, k) - lc, w);
+          }
+#pragma unroll
+          for (int c = 0; c < CW; ++c)
+            L[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
+                    (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
+        } else {
+          if (at) {
+            const float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
+            if (bp < 0 || g > bg) {
+              bg = g;
+              bp = p0 + j;
+              my_nl = nl;
+              my_sl = sl;
+            }
+          }
+          sl += s_q[wb][e] * (long long)w;
         }
+        nl += w;
+      }
+      if (P.task == 0) {
+        bg = nb.gain(nd.n);
+        bp = nb.p;
       }
       // warp argmax: higher gain, then lower position
       float wg = bg;
@@ -220,7 +270,8 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
         cd.valid = 1;
         cd.gain = wg;
         // entries at sorted positions wp-1 and wp
-        const unsigned long long ka = s_key[wb][wp - 1], kb = s_key[wb][wp];
+        const unsigned long long ka = s_key[wb][wp - 1 + (wp - 1) / E],
+                                 kb = s_key[wb][wp + wp / E];
         const float xa = __ldg(xf + s_row[wb][(int)(ka & 0xFFFFFFFFull)]);
         const float xb = __ldg(xf + s_row[wb][(int)(kb & 0xFFFFFFFFull)]);
         cd.thr = midpoint_threshold(xa, xb);
