@@ -69,9 +69,27 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
     if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     Cand best;
     best.valid = 0;
+    // the features of tries 0 .. 31, computed by the group's lanes at once
+    constexpr int NT = 32 / G;
+    const int ntry = P.n_mand + P.n_opt;
+    int fpre[NT];
+#pragma unroll
+    for (int r = 0; r < NT; ++r) fpre[r] = gl + G * r < ntry ? feature_of_try(P, nd, gl + G * r) : 0;
     for (int t = 0;; ++t) {
-      const int f = feature_of_try(P, nd, t);
+      int f;
+      if (t < 32) {
+        int fr = fpre[0];
+#pragma unroll
+        for (int r = 1; r < NT; ++r)
+          if (t / G == r) fr = fpre[r];
+        f = __shfl_sync(gm, fr, t % G, G);
+      } else {
+        f = feature_of_try(P, nd, t);
+      }
       const float* xf = P.X + (long long)f * P.N;
+      // RF with value ranks: rank << 5 | group lane as one 32-bit sort key
+      // (invalid lanes sort last with their own lane index)
+      const bool r32 = P.algo == 0 && P.rank != nullptr && P.N <= (1ll << 26);
       const float xv = valid ? __ldg(xf + row) : 0.0f;
       Cand cd;
       cd.f = f;
@@ -117,21 +135,41 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
           cd.gain = cd.valid ? variance_gain(nl, sl, nr, nd.sum - sl, P.S) : -FLT_MAX;
         }
       } else {  // RF: bitonic sort of (key, lane) over the group
-        uint32_t key = valid ? orderable(xv) : 0xFFFFFFFFu;
-        int idx = gl;
+        uint32_t key;
+        int idx;
+        if (r32) {
+          uint32_t pk32 = valid ? (__ldg(P.rank + (long long)f * P.N + row) << 5) | (uint32_t)gl
+                                : 0xFFFFFFE0u | (uint32_t)gl;
 #pragma unroll
-        for (int kk = 2; kk <= G; kk <<= 1) {
+          for (int kk = 2; kk <= G; kk <<= 1) {
 #pragma unroll
-          for (int j = kk >> 1; j > 0; j >>= 1) {
-            uint32_t pk = __shfl_xor_sync(gm, key, j, G);
-            int pi = __shfl_xor_sync(gm, idx, j, G);
-            bool up = (gl & kk) == 0;
-            bool lower = (gl & j) == 0;
-            bool mine_smaller = key < pk || (key == pk && idx < pi);
-            bool keep = (lower == up) ? mine_smaller : !mine_smaller;
-            if (!keep) {
-              key = pk;
-              idx = pi;
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+              const uint32_t o = __shfl_xor_sync(gm, pk32, j, G);
+              const bool up = (gl & kk) == 0;
+              const bool lower = (gl & j) == 0;
+              const uint32_t mn = min(pk32, o), mx = max(pk32, o);
+              pk32 = (lower == up) ? mn : mx;
+            }
+          }
+          key = gl < m ? pk32 >> 5 : 0xFFFFFFFFu;
+          idx = (int)(pk32 & 31u);
+        } else {
+          key = valid ? orderable(xv) : 0xFFFFFFFFu;
+          idx = gl;
+#pragma unroll
+          for (int kk = 2; kk <= G; kk <<= 1) {
+#pragma unroll
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+              uint32_t pk = __shfl_xor_sync(gm, key, j, G);
+              int pi = __shfl_xor_sync(gm, idx, j, G);
+              bool up = (gl & kk) == 0;
+              bool lower = (gl & j) == 0;
+              bool mine_smaller = key < pk || (key == pk && idx < pi);
+              bool keep = (lower == up) ? mine_smaller : !mine_smaller;
+              if (!keep) {
+                key = pk;
+                idx = pi;
+              }
             }
           }
         }

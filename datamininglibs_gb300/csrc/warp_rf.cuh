@@ -12,8 +12,8 @@
 
 namespace dml {
 
-template <int E>
-__device__ __forceinline__ void warp_bitonic_sort(unsigned long long (&key)[E]) {
+template <int E, class T>
+__device__ __forceinline__ void warp_bitonic_sort(T (&key)[E]) {
   const int lane = threadIdx.x & 31;
   constexpr int M = 32 * E;
 #pragma unroll
@@ -28,7 +28,7 @@ __device__ __forceinline__ void warp_bitonic_sort(unsigned long long (&key)[E]) 
           if (p > r) {
             const int i = r * 32 + lane;
             const bool up = (i & k) == 0;
-            unsigned long long a = key[r], b = key[p];
+            T a = key[r], b = key[p];
             bool swap = up ? (a > b) : (a < b);
             key[r] = swap ? b : a;
             key[p] = swap ? a : b;
@@ -40,11 +40,11 @@ __device__ __forceinline__ void warp_bitonic_sort(unsigned long long (&key)[E]) 
           const int i = r * 32 + lane;
           const bool up = (i & k) == 0;
           const bool lower = (lane & j) == 0;
-          unsigned long long o = __shfl_xor_sync(kFull, key[r], j);
-          unsigned long long mine = key[r];
+          T o = __shfl_xor_sync(kFull, key[r], j);
+          T mine = key[r];
           // the lower element keeps the min of an ascending pair
           bool take_min = (lower == up);
-          unsigned long long mn = mine < o ? mine : o, mx = mine < o ? o : mine;
+          T mn = mine < o ? mine : o, mx = mine < o ? o : mine;
           key[r] = take_min ? mn : mx;
         }
       }
@@ -102,6 +102,10 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
     const int m = nd.ecnt;
     const int* ncnt = a.cnt + (long long)node * a.Cmax;
     const int ml = max(1, P.min_leaf);
+    // sort keys: rank << kIdxBits | entry when ranks and entries fit 31 bits
+    constexpr int kIdxBits = E == 2 ? 6 : E == 4 ? 7 : E == 8 ? 8 : 9;
+    static_assert((1 << kIdxBits) == M, "entry index bits");
+    const bool r32 = P.rank != nullptr && (32 - __clz((int)max(1ll, P.N - 1))) + kIdxBits <= 31;
     int rowr[E];
 #pragma unroll
     for (int r = 0; r < E; ++r) {
@@ -129,20 +133,40 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs 
     unsigned long long bestL[CW];
 #pragma unroll
     for (int j = 0; j < CW; ++j) bestL[j] = 0;
+    // the features of tries 0 .. 31, one per lane
+    const int fpre = lane < P.n_mand + P.n_opt ? feature_of_try(P, nd, lane) : 0;
     int t = 0;
     for (;; ++t) {
-      const int f = feature_of_try(P, nd, t);
+      const int f = t < 32 ? __shfl_sync(kFull, fpre, t) : feature_of_try(P, nd, t);
       const float* xf = P.X + (long long)f * P.N;
-      unsigned long long key[E];
+      if (r32) {
+        // value ranks and entry indices packed in 32 bits: half the shuffles
+        const uint32_t* rk = P.rank + (long long)f * P.N;
+        uint32_t key[E];
 #pragma unroll
-      for (int r = 0; r < E; ++r) {
-        const int i = r * 32 + lane;
-        key[r] = i < m ? (((unsigned long long)orderable(__ldg(xf + rowr[r])) << 32) | (unsigned)i)
-                       : ~0ull;
+        for (int r = 0; r < E; ++r) {
+          const int i = r * 32 + lane;
+          key[r] = i < m ? (__ldg(rk + rowr[r]) << kIdxBits) | (uint32_t)i : ~0u;
+        }
+        warp_bitonic_sort<E>(key);
+#pragma unroll
+        for (int r = 0; r < E; ++r)
+          s_key[wb][r * 32 + lane + (r * 32 + lane) / E] =
+              key[r] == ~0u ? ~0ull
+                            : ((unsigned long long)(key[r] >> kIdxBits) << 32) |
+                                  (key[r] & (uint32_t)(M - 1));
+      } else {
+        unsigned long long key[E];
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          const int i = r * 32 + lane;
+          key[r] = i < m ? (((unsigned long long)orderable(__ldg(xf + rowr[r])) << 32) | (unsigned)i)
+                         : ~0ull;
+        }
+        warp_bitonic_sort<E>(key);
+#pragma unroll
+        for (int r = 0; r < E; ++r) s_key[wb][r * 32 + lane + (r * 32 + lane) / E] = key[r];
       }
-      warp_bitonic_sort<E>(key);
-#pragma unroll
-      for (int r = 0; r < E; ++r) s_key[wb][r * 32 + lane + (r * 32 + lane) / E] = key[r];
       __syncwarp();
       // boundary scan: lane l owns sorted positions l*E .. l*E+E-1.  One warp
       // scan of the lanes' row counts and packed class counts (or target
