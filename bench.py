@@ -327,8 +327,8 @@ def run_ours(args, w):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # scheduling picked by the autotuner on an 8-tree sample (untimed)
-    tuning = None if args.no_tune else dml.autotune(Xd, yd, sample_trees=8, stream=stream, **kw)
+    # scheduling picked by the autotuner on a 32-tree sample (untimed)
+    tuning = None if args.no_tune else dml.autotune(Xd, yd, sample_trees=32, stream=stream, **kw)
     for _ in range(args.warmup):
         dml.fit(Xd, yd, stream=stream, **kw).free()
     barrier()

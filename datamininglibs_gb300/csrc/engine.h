@@ -52,8 +52,8 @@ dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s);
 constexpr int kSearchSmemCap = 4096;
 constexpr int kDefaultSmemCap = 2048;
 
-// Scheduling of a fit (tuning.cu): RF nodes of up to warp_max entries (64, 128
-// or 256) are searched by a warp, up to smem_cap by a CTA in shared memory,
+// Scheduling of a fit (tuning.cu): RF nodes of up to warp_max entries (64, 128,
+// 256 or 512) are searched by a warp, up to smem_cap by a CTA in shared memory,
 // larger ones as per-try items on big_ctas persistent CTAs per SM.
 struct Tuning {
   int warp_max, smem_cap, big_ctas;

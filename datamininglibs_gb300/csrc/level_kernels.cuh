@@ -282,13 +282,13 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
 // memory sort), RF big (CTA, global sort).  Queue order does not affect
 // results, only scheduling.
 enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kQRfW2 = 4, kQRfW4 = 5, kQRfW8 = 6,
-       kQG16 = 7, kQG8 = 8, kNumQ = 9 };
+       kQG16 = 7, kQG8 = 8, kQRfW16 = 9, kNumQ = 10 };
 
 struct Queues {
   int* list[kNumQ];
   int* count;  // [kNumQ]
   int rf_small_cap;  // RF nodes up to this many entries sort in shared memory
-  int rf_warp_max;   // RF nodes up to this many entries (64, 128 or 256) sort in a warp
+  int rf_warp_max;   // RF nodes up to this many entries (64, 128, 256 or 512) sort in a warp
 };
 
 // Warp-aggregated append of `node` to queue q (all lanes call; `want` selects).
@@ -316,6 +316,7 @@ __device__ __forceinline__ int queue_of(const ProbDesc& P, int ecnt, const Queue
   if (ecnt <= 64 && Q.rf_warp_max >= 64) return kQRfW2;
   if (ecnt <= 128 && Q.rf_warp_max >= 128) return kQRfW4;
   if (ecnt <= 256 && Q.rf_warp_max >= 256) return kQRfW8;
+  if (ecnt <= 512 && Q.rf_warp_max >= 512) return kQRfW16;
   return ecnt <= Q.rf_small_cap ? kQRfSmall : kQRfBig;
 }
 

@@ -45,6 +45,9 @@ void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s) {
     k_warp_rf<4, CW><<<wblocks, 256, 0, s>>>(b);
   } else if (q == kQRfW8) {
     k_warp_rf<8, CW><<<wblocks, 256, 0, s>>>(b);
+  } else if (q == kQRfW16) {
+    constexpr int wpb = warp_rf_wpb<16>();
+    k_warp_rf<16, CW><<<std::max(1, std::min((count + wpb - 1) / wpb, 1 << 20)), 32 * wpb, 0, s>>>(b);
   } else if (q == kQErt) {
     k_ert_cta<kBlock><<<std::min(count, 1 << 20), kBlock, 0, s>>>(b);
   } else {

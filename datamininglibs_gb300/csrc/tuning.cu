@@ -84,11 +84,12 @@ int class_width(int C) {
 }
 
 bool valid_tuning(const Tuning& t) {
-  return (t.warp_max == 64 || t.warp_max == 128 || t.warp_max == 256) && t.smem_cap >= 257 &&
+  return (t.warp_max == 64 || t.warp_max == 128 || t.warp_max == 256 || t.warp_max == 512) &&
+         t.smem_cap >= 257 &&
          t.smem_cap <= kSearchSmemCap && t.big_ctas >= 1 && t.big_ctas <= 3;
 }
 
-Tuning default_tuning(int CW) { return Tuning{256, kDefaultSmemCap, big_ctas_per_sm(CW)}; }
+Tuning default_tuning(int CW) { return Tuning{512, kDefaultSmemCap, big_ctas_per_sm(CW)}; }
 
 // The tuning of a fit: the forced candidate, the stored tuning of the largest
 // problem's bucket, or the defaults.
@@ -140,9 +141,10 @@ dml_status dml_autotune(const dml_fit_desc* desc, int32_t sample_trees, dml_tuni
   const int max_ctas = default_tuning(class_width(C)).big_ctas;
   std::vector<Tuning> cands;
   if (d.algo == DML_ALGO_RF) {
-    for (int wm : {128, 256})
-      for (int cap : {2048, kSearchSmemCap})
-        for (int bc = 1; bc <= max_ctas; ++bc) cands.push_back(Tuning{wm, cap, bc});
+    for (int wm : {256, 512})
+      for (int cap : {1024, 2048, kSearchSmemCap})
+        for (int bc = std::max(1, max_ctas - 1); bc <= max_ctas; ++bc)
+          cands.push_back(Tuning{wm, cap, bc});
   } else {
     cands.push_back(default_tuning(class_width(C)));  // ERT has no RF thresholds
   }

@@ -72,14 +72,21 @@ __device__ __forceinline__ int Nt_of(const int (&Nt)[2 * CW], int c) {
   return x;
 }
 
-// Warps per block: 8, or 4 for 512-entry nodes (shared memory per warp).
+// Warps per block: 8, or 2 for 512-entry nodes (static shared memory per warp).
 template <int E>
 constexpr int warp_rf_wpb() {
-  return E >= 16 ? 4 : 8;
+  return E >= 16 ? 2 : 8;
+}
+
+// At most 128 registers a thread: 16 warps of an SM.
+template <int E>
+constexpr int warp_rf_min_blocks() {
+  return 16 / warp_rf_wpb<E>();
 }
 
 template <int E, int CW>
-__global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), 2) k_warp_rf(LevelArgs a) {
+__global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>())
+    k_warp_rf(LevelArgs a) {
   constexpr int M = 32 * E;
   constexpr int WPB = warp_rf_wpb<E>();
   __shared__ int s_row[WPB][M];

@@ -100,14 +100,16 @@ typedef struct {
 enum {
   DML_Q_WARP32 = 0,   /* <= 32 entries, one warp per node (k_group_nodes<32>) */
   DML_Q_ERT = 1,      /* ERT, > 32 entries, one CTA per node (k_ert_cta) */
-  DML_Q_RF_SMEM = 2,  /* RF, 257..4096 entries, CTA, shared-memory sort (k_rf_smem) */
+  DML_Q_RF_SMEM = 2,  /* RF, above the warp classes up to the tuned cap (at most 4096
+                       * entries), CTA, shared-memory sort (k_rf_smem) */
   DML_Q_RF_BIG = 3,   /* RF, > 4096 entries, per-try items (k_rf_big_items + _decide) */
   DML_Q_RF_W64 = 4,   /* RF, 33..64 entries, warp register sort (k_warp_rf<2>) */
   DML_Q_RF_W128 = 5,  /* RF, 65..128 entries (k_warp_rf<4>) */
   DML_Q_RF_W256 = 6,  /* RF, 129..256 entries (k_warp_rf<8>) */
   DML_Q_GROUP16 = 7,  /* <= 16 entries, 16 lanes per node (k_group_nodes<16>) */
   DML_Q_GROUP8 = 8,   /* <= 8 entries, 8 lanes per node (k_group_nodes<8>) */
-  DML_NUM_QUEUES = 9
+  DML_Q_RF_W512 = 9,  /* RF, 257..512 entries (k_warp_rf<16>) */
+  DML_NUM_QUEUES = 10
 };
 
 /* Fit statistics of the last dml_fit/dml_fit_batched on this thread. */

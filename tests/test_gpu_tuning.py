@@ -30,7 +30,8 @@ np.save(sys.argv[2], nodes)
 """
 
 
-@pytest.mark.parametrize("tuning", [(64, 300, 1), (128, 2048, 2), (256, 4096, 2)])
+@pytest.mark.parametrize("tuning", [(64, 300, 1), (128, 2048, 2), (256, 4096, 2),
+                                    (512, 1024, 3)])
 def test_forced_tunings_give_the_oracle_forest(tmp_path, tuning):
     X, y = synth.rf_multiclass(20000, 12, n_classes=3, n_int=3, seed=8)
     m = oracle.fit(X, y, **KW)
