@@ -200,21 +200,29 @@ struct BigArgs {
   int* nretry_out;
   int* big_index;          // node id -> index in `big` (for phase 2)
   uint32_t* pv;            // classification: label << 27 | weight per entry slot of the big nodes
+  long long* pq;           // regression: fixed-point target per entry slot of the big nodes
 };
 
-// Packed (label << 27 | weight) values of the big classification nodes' entries,
-// once per level instead of a label gather per try.
+// Per-entry values of the big nodes, once per level instead of a gather by
+// row per try: packed (label << 27 | weight) for classification, the target
+// for regression.
 template <int CW>
 __global__ void __launch_bounds__(kBigBlock) k_big_pack(BigArgs b) {
   const LevelArgs& a = b.L;
   for (int ni = blockIdx.x; ni < b.nbig; ni += gridDim.x) {
     const LNode nd = a.nodes[b.big[ni]];
     const ProbDesc& P = a.probs[nd.prob];
-    if (P.task != 0) continue;
-    for (int i = threadIdx.x; i < nd.ecnt; i += kBigBlock) {
-      const long long e = nd.ebeg + i;
-      b.pv[e] = ((uint32_t)__ldg(P.lab + __ldg(a.rowsA + e)) << 27) |
-                (uint32_t)(a.wA ? __ldg(a.wA + e) : 1);
+    if (P.task == 0 && b.pv) {
+      for (int i = threadIdx.x; i < nd.ecnt; i += kBigBlock) {
+        const long long e = nd.ebeg + i;
+        b.pv[e] = ((uint32_t)__ldg(P.lab + __ldg(a.rowsA + e)) << 27) |
+                  (uint32_t)(a.wA ? __ldg(a.wA + e) : 1);
+      }
+    } else if (P.task != 0 && b.pq) {
+      for (int i = threadIdx.x; i < nd.ecnt; i += kBigBlock) {
+        const long long e = nd.ebeg + i;
+        b.pq[e] = __ldg(P.q + __ldg(a.rowsA + e));
+      }
     }
   }
 }
@@ -473,12 +481,8 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     const bool in2 = big_sort(k1, v1, k2, v2, m, diff, S);
     const uint32_t* sk = in2 ? k2 : k1;
     const uint32_t* sv = in2 ? v2 : v1;
-    // regression: per-entry targets in the free pair buffer (8 bytes per entry)
-    long long* eq = (long long*)(in2 ? k1 : k2);
-    if (!packed) {
-      for (int i = threadIdx.x; i < m; i += kBigBlock) eq[i] = __ldg(P.q + __ldg(rows + i));
-      __syncthreads();
-    }
+    // regression: the node's per-entry targets
+    const long long* eq = b.pq + nd.ebeg;
     float g;
     int p;
     long long nl, sl;

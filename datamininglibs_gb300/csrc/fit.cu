@@ -453,10 +453,15 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     }
     uint32_t* big_slot =
         slot_stride > 0 ? (uint32_t*)alloc(sizeof(uint32_t) * 4 * slot_stride * big_grid) : nullptr;
-    bool any_cls = false;
-    for (auto& P : hp) any_cls = any_cls || P.task == 0;
+    bool any_cls = false, any_reg = false;
+    for (auto& P : hp) {
+      any_cls = any_cls || P.task == 0;
+      any_reg = any_reg || P.task != 0;
+    }
     uint32_t* big_pv =
         slot_stride > 0 && any_cls ? (uint32_t*)alloc(sizeof(uint32_t) * total_slots) : nullptr;
+    long long* big_pq =
+        slot_stride > 0 && any_reg ? (long long*)alloc(sizeof(long long) * total_slots) : nullptr;
     int* d_nretry = (int*)alloc(sizeof(int));
     ProbDesc* d_probs = (ProbDesc*)alloc(sizeof(ProbDesc) * nprob);
     DML_CK(cudaMemcpyAsync(d_probs, hp.data(), sizeof(ProbDesc) * nprob, cudaMemcpyHostToDevice, s));
@@ -585,6 +590,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           b.nretry_out = d_nretry;
           b.big_index = big_index.p;
           b.pv = big_pv;
+          b.pq = big_pq;
           DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
           b.L.stats = d_stats + 4 + 4 * q;
           DML_CK(cudaEventRecord(qev[q][0], s));
@@ -595,8 +601,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
             DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
             launch_big(CW, b, 1, big_grid, std::min(b.nbig, 65535), max_mand, s);
             launch_big(CW, b, 2, big_grid, std::min(b.nbig, 65535), std::max(1, max_opt), s);
-            st.launches += big_pv ? 5 : 4;
-            queue_launches[q] += big_pv ? 5 : 4;
+            st.launches += 5;
+            queue_launches[q] += 5;
             if (plain) DML_CK(cudaStreamSynchronize(s));
           }
           DML_CK(cudaEventRecord(qev[q][1], s));

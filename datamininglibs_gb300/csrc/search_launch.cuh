@@ -61,7 +61,7 @@ template <int CW>
 void launch_big_cw(BigArgs b, int phase, int grid, int decide_grid, int tries, cudaStream_t s) {
   b.phase = phase;
   b.tries_per_node = tries;
-  if (phase == 1 && b.pv) k_big_pack<CW><<<decide_grid, kBigBlock, 0, s>>>(b);
+  if (phase == 1) k_big_pack<CW><<<decide_grid, kBigBlock, 0, s>>>(b);
   k_rf_big_items<CW><<<grid, kBigBlock, 0, s>>>(b);
   k_rf_big_decide<CW><<<decide_grid, kBigBlock, 0, s>>>(b);
   DML_CK(cudaGetLastError());
