@@ -67,6 +67,17 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
 #pragma unroll
     for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
     if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
+    // RF classification: h(n), the class total of each lane's entry and the
+    // bit planes of the group's largest weight, fixed across tries
+    const long long Hn = P.task == 0 ? __ldg(a.H + nd.n) : 0;
+    const int Nk = (P.task == 0 && valid) ? __ldg(ncnt + k) : 0;
+    int wbits;
+    {
+      int wm = w;
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(gm, wm, o, G));
+      wbits = 32 - __clz(max(wm, 1));
+    }
     Cand best;
     best.valid = 0;
     // the features of tries 0 .. 31, computed by the group's lanes at once
@@ -186,14 +197,24 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
         float g = -FLT_MAX;
         long long sl = 0;
         if (P.task == 0) {
-          int L[2 * CW];
-#pragma unroll
-          for (int c = 0; c < 2 * CW; ++c)
-            L[c] = c < C ? grp_excl_scan<G, int>(ke == c ? we : 0, gl, gm) : 0;
-          if (bnd)
-            g = entropy_gain_u<2 * CW>(
-                a.H, prior, C, nl, nr, [&](int c) { return (long long)L[c]; },
-                [&](int c) { return (long long)Nt[c]; });
+          // gain numerator P - Q = h(n) - h(nL) - h(nR) + sum over the positions q
+          // left of the boundary of the change that moving q's entry to the left
+          // makes to sum_c h(L_c) + h(N_c - L_c): only its own class c changes,
+          // from L_c (the weight of class c at positions below q: the lanes
+          // matching its class, summed over the weights' bit planes)
+          const int Ne = __shfl_sync(gm, Nk, idx, G);
+          const bool ve = gl < m;
+          const unsigned below = __match_any_sync(gm, ve ? ke : -1) & glt;
+          int Lo = 0;
+          for (int b = 0; b < wbits; ++b)
+            Lo += __popc(__ballot_sync(gm, (we >> b) & 1) & below) << b;
+          long long dq = 0;
+          if (ve) {
+            const int R = Ne - Lo;
+            dq = (__ldg(a.H + Lo + we) - __ldg(a.H + Lo)) + (__ldg(a.H + R - we) - __ldg(a.H + R));
+          }
+          const long long S = grp_excl_scan<G, long long>(dq, gl, gm);
+          if (bnd) g = gain_from_numerator(Hn - __ldg(a.H + nl) - __ldg(a.H + nr) + S, nd.n);
         } else {
           sl = grp_excl_scan<G, long long>(qe * (long long)we, gl, gm);
           if (bnd) g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
