@@ -2,7 +2,7 @@
 // admission.  No reference counterpart (the reference predicts one data frame
 // per call, gpudte_algorithm.cc:270-331).
 //
-// One worker thread drives two lanes, each with n_streams batch slots:
+// Two lanes, each with n_streams batch slots and its own worker thread:
 //  * small lane (requests of at most small_rows rows): high-priority streams;
 //    a batch packs whole requests of any forests into 16-row tiles whose rows
 //    are walked by 8 threads each (one eighth of the trees per thread), which
@@ -199,7 +199,7 @@ struct dml_server {
   long long small_rows = 4096;
   std::vector<const dml_forest*> forests;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work[2], cv_done;  // cv_work[1]: small lane, [0]: large lane
   std::deque<std::shared_ptr<dml::Request>> q_small, q_large;
   std::unordered_map<long long, double> done;  // id -> latency ms
   std::vector<double> latencies;
@@ -207,7 +207,7 @@ struct dml_server {
   dml::Clock::time_point first_submit, last_done;
   bool have_first = false, stop = false;
   std::vector<dml::Slot> slots;  // n_streams small-lane slots, then n_streams large-lane
-  std::thread worker;
+  std::thread worker[2];  // [1] drives the small lane's slots, [0] the large lane's
   size_t small_cap = 0, large_cap = 0;
 };
 
@@ -230,11 +230,11 @@ bool split_ok(const dml_forest* f) {
          (f->task == DML_CLASSIFICATION || f->n_trees <= kSplitMaxTrees);
 }
 
-// Completes finished batches; returns true if any slot finished.
-bool reap(dml_server* s) {
+// Completes the lane's finished batches; returns true if any slot finished.
+bool reap(dml_server* s, bool small) {
   bool any = false;
   for (Slot& sl : s->slots) {
-    if (!sl.batch.busy) continue;
+    if (sl.small != small || !sl.batch.busy) continue;
     if (cudaEventQuery(sl.batch.done) != cudaSuccess) continue;
     for (const Piece& p : sl.batch.pieces) {
       const Request& r = *p.req;
@@ -379,44 +379,47 @@ bool launch_batch(dml_server* s, Slot& sl) {
   return true;
 }
 
-void worker_main(dml_server* s) {
+// One worker per lane, so that the small lane's launches and completions never
+// wait behind the large lane's host work (staging, result copies).
+void worker_main(dml_server* s, bool small) {
   cudaSetDevice(s->device);
+  auto& q = small ? s->q_small : s->q_large;
+  auto& cv = s->cv_work[small ? 1 : 0];
   while (true) {
-    bool progressed = reap(s);
-    bool small_idle = true;
+    bool progressed = reap(s, small);
+    bool idle = true;
     for (Slot& sl : s->slots)
-      if (sl.small) small_idle = small_idle && !sl.batch.busy;
+      if (sl.small == small) idle = idle && !sl.batch.busy;
     for (Slot& sl : s->slots) {
-      if (sl.batch.busy) continue;
+      if (sl.small != small || sl.batch.busy) continue;
       bool pending;
       {
         std::lock_guard<std::mutex> lk(s->mu);
-        pending = !(sl.small ? s->q_small : s->q_large).empty();
+        pending = !q.empty();
       }
       if (!pending) continue;
-      if (sl.small && small_idle && s->cfg.max_wait_us > 0) {
+      if (small && idle && s->cfg.max_wait_us > 0) {
         // an idle lane lets a batch fill briefly while few rows wait
         std::unique_lock<std::mutex> lk(s->mu);
         long long waiting = 0;
-        for (auto& r : s->q_small) waiting += r->n - r->next_row;
+        for (auto& r : q) waiting += r->n - r->next_row;
         if (waiting < s->small_rows)
-          s->cv_work.wait_for(lk, std::chrono::microseconds(s->cfg.max_wait_us));
-        small_idle = false;
+          cv.wait_for(lk, std::chrono::microseconds(s->cfg.max_wait_us));
+        idle = false;
       }
       progressed |= launch_batch(s, sl);
     }
     bool any_busy = false;
-    for (Slot& sl : s->slots) any_busy |= sl.batch.busy;
+    for (Slot& sl : s->slots)
+      if (sl.small == small) any_busy |= sl.batch.busy;
     std::unique_lock<std::mutex> lk(s->mu);
-    const bool queued = !s->q_small.empty() || !s->q_large.empty();
-    if (s->stop && !queued && !any_busy) break;
+    if (s->stop && q.empty() && !any_busy) break;
     if (!progressed) {
       if (any_busy) {
         lk.unlock();
         std::this_thread::sleep_for(std::chrono::microseconds(10));
       } else {
-        s->cv_work.wait_for(lk, std::chrono::milliseconds(5),
-                            [&] { return s->stop || !s->q_small.empty() || !s->q_large.empty(); });
+        cv.wait_for(lk, std::chrono::milliseconds(5), [&] { return s->stop || !q.empty(); });
       }
     }
   }
@@ -476,7 +479,8 @@ dml_status dml_server_create(const dml_server_config* cfg, dml_server** out) {
     dml_server_destroy(s);
     return DML_ERR_OOM;
   }
-  s->worker = std::thread(worker_main, s);
+  s->worker[0] = std::thread(worker_main, s, false);
+  s->worker[1] = std::thread(worker_main, s, true);
   *out = s;
   return DML_OK;
 }
@@ -514,6 +518,7 @@ dml_status dml_server_submit(dml_server* s, int32_t forest_id, const float* samp
       cudaGetLastError();
     }
   }
+  bool to_small = false;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (forest_id < 0 || forest_id >= (int32_t)s->forests.size()) {
@@ -549,8 +554,9 @@ dml_status dml_server_submit(dml_server* s, int32_t forest_id, const float* samp
     }
     (small_fit ? s->q_small : s->q_large).push_back(r);
     *request_id = r->id;
+    to_small = small_fit;
   }
-  s->cv_work.notify_one();
+  s->cv_work[to_small ? 1 : 0].notify_one();
   return DML_OK;
 }
 
@@ -615,8 +621,9 @@ void dml_server_destroy(dml_server* s) {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
   }
-  s->cv_work.notify_all();
-  if (s->worker.joinable()) s->worker.join();
+  for (auto& cv : s->cv_work) cv.notify_all();
+  for (auto& w : s->worker)
+    if (w.joinable()) w.join();
   for (Slot& sl : s->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
     if (sl.batch.done) cudaEventDestroy(sl.batch.done);
