@@ -231,7 +231,10 @@ __global__ void __launch_bounds__(kBigBlock) k_big_pack(BigArgs b) {
 // elements of every tile of 256 * per.  Classification items carry
 // (label << 27 | weight) through the sort (packed == true); regression items
 // carry the entry index into ew / eq.
-template <int CW>
+// INCR (classification): each thread keeps its values in registers and Q
+// incrementally along its elements (6 table terms an entry instead of 2C + 2
+// a boundary); worth it for 8 elements per thread.
+template <int CW, bool INCR>
 __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed, const int* ew,
                              const long long* eq, int m, int per, const LNode& nd,
                              const ProbDesc& P, const int* ncnt, const long long* H, long long prior,
@@ -268,15 +271,18 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
     uint32_t kk[kBigPer];
     int w[kBigPer];
     long long q[kBigPer];
+    uint32_t vq[kBigPer];  // INCR: the packed values, consumed from vq[0]
     unsigned bnd = 0;  // classification: bit j set when element j starts a new key
     if (packed) {
       uint32_t prev = prevk0;
 #pragma unroll
       for (int j = 0; j < kBigPer; ++j) {
         const int p = p0 + j;
+        vq[j] = 0;
         if (j < per && p < m) {
           const uint32_t kj = sk[p];
           const uint32_t vv = sv[p];
+          vq[j] = vv;
           if (p > 0 && prev < kj) bnd |= 1u << j;
           prev = kj;
           const int lj = (int)(vv >> 27);
@@ -330,7 +336,54 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
       for (int c = 0; c < CW; ++c) runL[c] = 0;
     }
     uint32_t prevk = prevk0;
-    if (packed) {
+    if (packed && INCR) {
+      // Q computed in full at the first boundary that meets min_leaf, then
+      // moved entry by entry while boundaries remain (h(nL), h(nR) carried)
+      long long Q = 0, hl = 0, hr = 0;
+      bool haveQ = false;
+#pragma unroll 1
+      for (int j = 0; j < per; ++j) {
+        const uint32_t vv = vq[0];
+#pragma unroll
+        for (int k = 0; k + 1 < kBigPer; ++k) vq[k] = vq[k + 1];
+        const int p = p0 + j;
+        const int labj = (int)(vv >> 27);
+        const int wj = (int)(vv & 0x7FFFFFFu);
+        const long long nr = (long long)nd.n - run_n;
+        if (((bnd >> j) & 1u) && run_n >= ml && nr >= ml) {
+          if (!haveQ) {
+            Q = entropy_q_u<2 * CW>(
+                H, C, run_n, nr,
+                [&](int c) {
+                  return (long long)((c & 1) ? (runL[c >> 1] >> 32) : (runL[c >> 1] & 0xFFFFFFFFull));
+                },
+                [&](int c) { return (long long)Nt[c]; });
+            hl = __ldg(H + run_n);
+            hr = __ldg(H + nr);
+            haveQ = true;
+          }
+          if (nb.offer(prior - Q, p, nd.n)) {
+            bnl = run_n;
+#pragma unroll
+            for (int c = 0; c < CW; ++c) bL[c] = runL[c];
+          }
+        }
+        if (haveQ && (bnd >> (j + 1)) != 0u) {
+          const long long lc = packed_get<CW>(runL, labj);
+          const long long rc = (long long)Nt_of<CW>(Nt, labj) - lc;
+          const long long hl1 = __ldg(H + run_n + wj), hr1 = __ldg(H + nr - wj);
+          Q += (hl1 - hl) + (hr1 - hr) - (__ldg(H + lc + wj) - __ldg(H + lc)) -
+               (__ldg(H + rc - wj) - __ldg(H + rc));
+          hl = hl1;
+          hr = hr1;
+        }
+        run_n += wj;
+#pragma unroll
+        for (int c = 0; c < CW; ++c)
+          runL[c] += (labj == 2 * c ? (unsigned long long)wj : 0ull) |
+                     (labj == 2 * c + 1 ? ((unsigned long long)wj << 32) : 0ull);
+      }
+    } else if (packed) {
       // classification: a rolled loop that re-reads each label|weight value
       // (the class terms unrolled eight times overflow the instruction cache);
       // boundaries are compared on their exact gain numerators P - Q
@@ -487,7 +540,7 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     int p;
     long long nl, sl;
     unsigned long long L[CW];
-    big_boundary<CW>(sk, sv, packed, wts, eq, m, kBigPer, nd, P, ncnt, a.H, s_prior, S.scan64, &g,
+    big_boundary<CW, true>(sk, sv, packed, wts, eq, m, kBigPer, nd, P, ncnt, a.H, s_prior, S.scan64, &g,
                      &p, &nl, &sl, L);
     const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
     if (bp >= 0 && p == bp) {
@@ -710,7 +763,7 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_smem(Leve
       int p;
       long long nl, sl;
       unsigned long long L[CW];
-      big_boundary<CW>(sk, sv, packed, wts, q_e, m, per, nd, P, ncnt, a.H, s_prior,
+      big_boundary<CW, false>(sk, sv, packed, wts, q_e, m, per, nd, P, ncnt, a.H, s_prior,
                        scan64, &g, &p, &nl, &sl, L);
       const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
       if (bp >= 0 && p == bp) {
