@@ -72,6 +72,75 @@ __global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict_
   }
 }
 
+// Rows in tiles of 16, their features staged in shared memory (a row reads
+// one feature per node on its paths: from global memory those reads scatter
+// over the whole sample matrix), 8 threads per row walking trees g, g + 8, ...
+// two in lockstep.  Votes meet in shared memory (integer counts, order-free);
+// regression keeps each tree's leaf value and one thread sums them in tree
+// order, as k_predict does.
+constexpr int kPSplit = 8;
+constexpr int kPRows = kPredBlock / kPSplit;  // 16
+
+template <int TASK>
+__global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __restrict__ nodes,
+                                                              int n_trees, int C, int F,
+                                                              const float* __restrict__ X,
+                                                              long long N, float* __restrict__ out) {
+  extern __shared__ float psm[];  // xs [F][kPRows], then votes [kPRows][C] or values [kPRows][n_trees]
+  const long long row0 = (long long)blockIdx.x * kPRows;
+  const int rows = N - row0 < kPRows ? (int)(N - row0) : kPRows;
+  const int g = threadIdx.x % kPSplit;
+  const int r = threadIdx.x / kPSplit;
+  float* xs = psm;
+  for (int e = threadIdx.x; e < F * kPRows; e += kPredBlock) {
+    const int f = e / kPRows, rr = e % kPRows;
+    xs[e] = rr < rows ? __ldg(X + (long long)f * N + row0 + rr) : 0.0f;
+  }
+  int* votes = reinterpret_cast<int*>(psm + F * kPRows);
+  float* vals = psm + F * kPRows + r * n_trees;
+  if (TASK == 0)
+    for (int i = threadIdx.x; i < kPRows * C; i += kPredBlock) votes[i] = 0;
+  __syncthreads();
+  if (r < rows) {
+    const int4* nd = reinterpret_cast<const int4*>(nodes);
+    int k = g;
+    for (; k + kPSplit < n_trees; k += 2 * kPSplit) {
+      int4 a = __ldg(nd + k), b = __ldg(nd + k + kPSplit);
+      while (a.x >= 0 || b.x >= 0) {
+        if (a.x >= 0) a = __ldg(nd + (goes_left(xs[a.y * kPRows + r], __int_as_float(a.z)) ? a.x : a.x + 1));
+        if (b.x >= 0) b = __ldg(nd + (goes_left(xs[b.y * kPRows + r], __int_as_float(b.z)) ? b.x : b.x + 1));
+      }
+      if (TASK == 0) {
+        atomicAdd(&votes[r * C + a.y], 1);
+        atomicAdd(&votes[r * C + b.y], 1);
+      } else {
+        vals[k] = __int_as_float(a.z);
+        vals[k + kPSplit] = __int_as_float(b.z);
+      }
+    }
+    if (k < n_trees) {
+      int4 a = __ldg(nd + k);
+      while (a.x >= 0)
+        a = __ldg(nd + (goes_left(xs[a.y * kPRows + r], __int_as_float(a.z)) ? a.x : a.x + 1));
+      if (TASK == 0)
+        atomicAdd(&votes[r * C + a.y], 1);
+      else
+        vals[k] = __int_as_float(a.z);
+    }
+  }
+  __syncthreads();
+  if (r < rows) {
+    const long long row = row0 + r;
+    if (TASK == 0) {
+      for (int c = g; c < C; c += kPSplit) out[row * C + c] = (float)votes[r * C + c];
+    } else if (g == 0) {
+      float sum = 0.0f;
+      for (int t = 0; t < n_trees; ++t) sum = __fadd_rn(sum, vals[t]);
+      out[row] = sum;
+    }
+  }
+}
+
 // The reference's predict structure (gpudte.cu:311-359): one thread per
 // (tree, row) of one tree; votes are added to the output (a launch holds each
 // row once, so plain adds keep tree order).
@@ -97,6 +166,25 @@ __global__ void k_predict_plain(const PNode* __restrict__ nodes, int tree, int C
 dml_status predict_device(const dml_forest* f, const float* dX, long long n_rows, float* dout,
                           cudaStream_t s) {
   if (n_rows <= 0) return DML_OK;
+  // staged rows when the tile (features, votes or per-tree values) fits 48 KB
+  const size_t split_sm =
+      sizeof(float) * kPRows *
+      ((size_t)f->n_features + (f->task == DML_CLASSIFICATION ? f->n_classes : f->n_trees));
+  if (split_sm <= 48 * 1024) {
+    const long long tiles = (n_rows + kPRows - 1) / kPRows;
+    if (f->task == DML_CLASSIFICATION)
+      k_predict_split<0><<<(unsigned)tiles, kPredBlock, split_sm, s>>>(
+          f->pnodes, f->n_trees, f->n_classes, f->n_features, dX, n_rows, dout);
+    else
+      k_predict_split<1><<<(unsigned)tiles, kPredBlock, split_sm, s>>>(
+          f->pnodes, f->n_trees, 1, f->n_features, dX, n_rows, dout);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error("predict launch failed: %s", cudaGetErrorString(e));
+      return DML_ERR_CUDA;
+    }
+    return DML_OK;
+  }
   const long long blocks = (n_rows + kPredBlock - 1) / kPredBlock;
   if (f->task == DML_CLASSIFICATION) {
     size_t sm = sizeof(int) * kPredBlock * f->n_classes;
