@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict_
 // Rows in tiles of 16, their features staged in shared memory (a row reads
 // one feature per node on its paths: from global memory those reads scatter
 // over the whole sample matrix), 8 threads per row walking trees g, g + 8, ...
-// two in lockstep.  Votes meet in shared memory (integer counts, order-free);
+// four in lockstep.  Votes meet in shared memory (integer counts, order-free);
 // regression keeps each tree's leaf value and one thread sums them in tree
 // order, as k_predict does.
 constexpr int kPSplit = 8;
@@ -103,29 +103,36 @@ __global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __res
   __syncthreads();
   if (r < rows) {
     const int4* nd = reinterpret_cast<const int4*>(nodes);
-    int k = g;
-    for (; k + kPSplit < n_trees; k += 2 * kPSplit) {
-      int4 a = __ldg(nd + k), b = __ldg(nd + k + kPSplit);
-      while (a.x >= 0 || b.x >= 0) {
-        if (a.x >= 0) a = __ldg(nd + (goes_left(xs[a.y * kPRows + r], __int_as_float(a.z)) ? a.x : a.x + 1));
-        if (b.x >= 0) b = __ldg(nd + (goes_left(xs[b.y * kPRows + r], __int_as_float(b.z)) ? b.x : b.x + 1));
+    // trees k, k + 8, k + 16, k + 24 in lockstep (four node loads in flight)
+    for (int k0 = g; k0 < n_trees; k0 += 4 * kPSplit) {
+      int4 lf[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = k0 + j * kPSplit;
+        lf[j] = k < n_trees ? __ldg(nd + k) : make_int4(-1, 0, 0, 0);
       }
-      if (TASK == 0) {
-        atomicAdd(&votes[r * C + a.y], 1);
-        atomicAdd(&votes[r * C + b.y], 1);
-      } else {
-        vals[k] = __int_as_float(a.z);
-        vals[k + kPSplit] = __int_as_float(b.z);
+      bool more = true;
+      while (more) {
+        more = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (lf[j].x >= 0) {
+            lf[j] = __ldg(nd + (goes_left(xs[lf[j].y * kPRows + r], __int_as_float(lf[j].z))
+                                    ? lf[j].x
+                                    : lf[j].x + 1));
+            more = more || lf[j].x >= 0;
+          }
       }
-    }
-    if (k < n_trees) {
-      int4 a = __ldg(nd + k);
-      while (a.x >= 0)
-        a = __ldg(nd + (goes_left(xs[a.y * kPRows + r], __int_as_float(a.z)) ? a.x : a.x + 1));
-      if (TASK == 0)
-        atomicAdd(&votes[r * C + a.y], 1);
-      else
-        vals[k] = __int_as_float(a.z);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = k0 + j * kPSplit;
+        if (k < n_trees) {
+          if (TASK == 0)
+            atomicAdd(&votes[r * C + lf[j].y], 1);
+          else
+            vals[k] = __int_as_float(lf[j].z);
+        }
+      }
     }
   }
   __syncthreads();
