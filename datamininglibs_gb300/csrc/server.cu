@@ -8,8 +8,9 @@
 //    are walked by 8 threads each (one eighth of the trees per thread), which
 //    cuts a row's chain of dependent node loads by 8;
 //  * large lane: low-priority streams; requests are cut into slices of at most
-//    max_batch_rows rows and a batch packs slices into 128-row tiles (one
-//    thread per row walks every tree).
+//    max_batch_rows rows and a batch packs slices into the same 16-row tiles
+//    (128-row tiles, one thread per row walking every tree, for forests whose
+//    rows or per-tree values do not fit a tile's shared memory).
 // Blocks of a low-priority launch are short (one tile), so a small batch waits
 // for at most one block per SM.  Requests that arrive while batches run join
 // the next batch of their lane as soon as a slot and budget free up.  A small
@@ -270,7 +271,11 @@ bool reap(dml_server* s, bool small) {
 bool launch_batch(dml_server* s, Slot& sl) {
   Batch& b = sl.batch;
   b.pieces.clear();
-  const int tile_rows = sl.small ? kSplitRows : kTileRows;
+  // rows per tile of a request's forest: 16-row staged tiles, 8 threads a row,
+  // wherever the forest allows them; 128-row tiles (a thread a row) otherwise
+  auto tile_rows_of = [&](const dml_forest* f) {
+    return sl.small || split_ok(f) ? kSplitRows : kTileRows;
+  };
   const long long max_rows = sl.small ? std::max<long long>(s->small_rows * 16, 65536)
                                       : s->cfg.max_batch_rows;
   size_t in_used = 0, out_used = 0;
@@ -281,6 +286,7 @@ bool launch_batch(dml_server* s, Slot& sl) {
     auto& q = sl.small ? s->q_small : s->q_large;
     while (!q.empty() && rows < max_rows) {
       std::shared_ptr<Request> r = q.front();
+      const int tile_rows = tile_rows_of(s->forests[r->forest]);
       const long long row_in = (long long)sizeof(float) * r->n_features;
       const long long row_out = (long long)sizeof(float) * r->width;
       // rows of this request that fit the batch's remaining room (64 rows of
@@ -309,14 +315,11 @@ bool launch_batch(dml_server* s, Slot& sl) {
   }
   if (b.pieces.empty()) return false;
   cudaStream_t st = sl.stream;
-  int nt = 0;
-  int shm = sizeof(int);
+  // inputs to the device
   for (const Piece& p : b.pieces) {
     const Request& r = *p.req;
-    const dml_forest* f = s->forests[r.forest];
     const bool direct = sl.small && r.mapped;
     char* d_stage = sl.d_in + p.in_off;
-    const float* d_x = direct ? r.d_samples : (const float*)d_stage;
     const size_t rb = sizeof(float) * p.rows;
     if (direct) {
       // the kernel reads the caller's buffer
@@ -335,31 +338,45 @@ bool launch_batch(dml_server* s, Slot& sl) {
           std::memcpy(h + rb * j, r.samples + (long long)j * r.n + p.row0, rb);
       cudaMemcpyAsync(d_stage, h, rb * r.n_features, cudaMemcpyHostToDevice, st);
     }
-    for (long long r0 = 0; r0 < p.rows; r0 += tile_rows) {
-      PredTile& t = sl.h_tiles[nt++];
-      t.nodes = f->pnodes;
-      t.X = d_x;
-      t.out = direct ? r.d_out : (float*)(sl.d_out + p.out_off);
-      t.n = direct ? r.n : p.rows;
-      t.row0 = (int)r0;
-      t.rows = (int)std::min<long long>(tile_rows, p.rows - r0);
-      t.n_trees = f->n_trees;
-      t.C = r.width;
-      t.task = f->task;
-      t.F = f->n_features;
+  }
+  // tiles: the staged (16-row) ones first, then the 128-row ones
+  int nt = 0, n_split = 0;
+  int shm_split = sizeof(int), shm_rows = sizeof(int);
+  for (int pass = 0; pass < 2; ++pass) {
+    for (const Piece& p : b.pieces) {
+      const Request& r = *p.req;
+      const dml_forest* f = s->forests[r.forest];
+      const int tile_rows = tile_rows_of(f);
+      if ((tile_rows == kSplitRows) != (pass == 0)) continue;
+      const bool direct = sl.small && r.mapped;
+      for (long long r0 = 0; r0 < p.rows; r0 += tile_rows) {
+        PredTile& t = sl.h_tiles[nt++];
+        t.nodes = f->pnodes;
+        t.X = direct ? r.d_samples : (const float*)(sl.d_in + p.in_off);
+        t.out = direct ? r.d_out : (float*)(sl.d_out + p.out_off);
+        t.n = direct ? r.n : p.rows;
+        t.row0 = (int)r0;
+        t.rows = (int)std::min<long long>(tile_rows, p.rows - r0);
+        t.n_trees = f->n_trees;
+        t.C = r.width;
+        t.task = f->task;
+        t.F = f->n_features;
+      }
+      if (pass == 0)
+        shm_split = std::max(
+            shm_split, (int)sizeof(int) * (kSplitRows * f->n_features +
+                                           (f->task == DML_CLASSIFICATION ? kSplitRows * r.width
+                                                                          : kSplitRows * f->n_trees)));
+      else
+        shm_rows = std::max(
+            shm_rows, (int)sizeof(int) * (f->task == DML_CLASSIFICATION ? kTileRows * r.width : 1));
     }
-    const int need =
-        sl.small ? kSplitRows * f->n_features + (f->task == DML_CLASSIFICATION
-                                                     ? kSplitRows * r.width
-                                                     : kSplitRows * f->n_trees)
-                 : (f->task == DML_CLASSIFICATION ? kTileRows * r.width : 1);
-    shm = std::max(shm, (int)sizeof(int) * need);
+    if (pass == 0) n_split = nt;
   }
   cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, sizeof(PredTile) * nt, cudaMemcpyHostToDevice, st);
-  if (sl.small)
-    k_predict_tiles_split<<<nt, kTileRows, shm, st>>>(sl.d_tiles);
-  else
-    k_predict_tiles<<<nt, kTileRows, shm, st>>>(sl.d_tiles);
+  if (n_split > 0) k_predict_tiles_split<<<n_split, kTileRows, shm_split, st>>>(sl.d_tiles);
+  if (nt > n_split)
+    k_predict_tiles<<<nt - n_split, kTileRows, shm_rows, st>>>(sl.d_tiles + n_split);
   for (const Piece& p : b.pieces) {
     const Request& r = *p.req;
     const size_t ob = sizeof(float) * p.rows * r.width;
@@ -461,8 +478,7 @@ dml_status dml_server_create(const dml_server_config* cfg, dml_server** out) {
     sl.cap = sl.small ? s->small_cap : s->large_cap;
     const long long lane_rows = sl.small ? std::max<long long>(s->small_rows * 16, 65536)
                                          : cfg->max_batch_rows;
-    sl.tile_cap = (int)std::min<long long>(
-        1 << 22, lane_rows / (sl.small ? kSplitRows : kTileRows) + 1024);
+    sl.tile_cap = (int)std::min<long long>(1 << 22, lane_rows / kSplitRows + 1024);
     ok = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking,
                                       sl.small ? prio_high : prio_low) == cudaSuccess &&
          cudaMallocHost(&sl.h_in, sl.cap) == cudaSuccess &&
