@@ -666,7 +666,7 @@ __global__ void __launch_bounds__(kBigBlock) k_rf_big_decide(BigArgs b) {
 //   classification: k1 v1 k2 v2 (sort buffers), row ids, packed values;
 //   regression:     k1 v1 k2 v2, fixed-point targets (8 bytes).
 template <int CW, int SMEM_CAP>
-__global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_smem(LevelArgs a) {
+__global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(LevelArgs a) {
   __shared__ SortSmem<kBigBlock> SS;
   __shared__ unsigned red[2 * kBigWarps];
   __shared__ unsigned long long scan64[kBigWarps * (CW + 1)];

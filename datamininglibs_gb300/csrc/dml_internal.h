@@ -7,10 +7,16 @@ namespace dml {
 constexpr int kMaxClasses = 32;
 constexpr int kMaxTries = 64;  // mandatory + optional tries evaluated per node
 
-// Resident CTAs per SM of the big-node item kernel: three (80 registers, a
-// few hundred bytes of spills that the extra warps more than pay for) up to
-// 16 classes, two for wider class counts.
-constexpr int big_ctas_per_sm(int cw) { return cw <= 8 ? 3 : 2; }
+// Resident CTAs per SM of the big-node item kernel: four (64 registers) for 3
+// to 16 classes, where the extra warps more than pay for the spills; three
+// (80 registers) for one packed word (two classes, or regression, whose
+// boundary scan keeps more per thread: four measured 3% slower there); two for
+// wider class counts.
+constexpr int big_ctas_per_sm(int cw) { return cw == 1 ? 3 : cw <= 8 ? 4 : 2; }
+
+// Resident CTAs per SM of the shared-memory search kernel (80 registers and
+// 59 KB of shared memory at the default cap of 2048 entries).
+constexpr int smem_ctas_per_sm(int cw) { return cw <= 8 ? 3 : 2; }
 
 // One forest of a fit batch (device-visible copy).
 struct ProbDesc {

@@ -86,7 +86,7 @@ int class_width(int C) {
 bool valid_tuning(const Tuning& t) {
   return (t.warp_max == 64 || t.warp_max == 128 || t.warp_max == 256 || t.warp_max == 512) &&
          t.smem_cap >= 257 &&
-         t.smem_cap <= kSearchSmemCap && t.big_ctas >= 1 && t.big_ctas <= 3;
+         t.smem_cap <= kSearchSmemCap && t.big_ctas >= 1 && t.big_ctas <= 4;
 }
 
 Tuning default_tuning(int CW) { return Tuning{512, kDefaultSmemCap, big_ctas_per_sm(CW)}; }

@@ -171,9 +171,10 @@ DML_API dml_status dml_fit_noalloc(const dml_fit_desc* desc, void* node_array,
 DML_API dml_status dml_last_fit_stats(dml_fit_stats* stats);
 
 /* Scheduling of RF fits (no counterpart in the reference): nodes of up to
- * warp_max entries (64, 128 or 256) are searched by one warp, up to smem_cap
- * entries (257 .. 4096) by one CTA in shared memory, larger ones as per-try
- * items on big_ctas_per_sm persistent CTAs per SM.  Results do not depend on
+ * warp_max entries (64, 128, 256 or 512) are searched by one warp, up to
+ * smem_cap entries (257 .. 4096) by one CTA in shared memory, larger ones as
+ * per-try items on big_ctas_per_sm (1 .. 4, at most what the item kernel's
+ * registers allow) persistent CTAs per SM.  Results do not depend on
  * it.  dml_autotune fits the first sample_trees trees of desc once per
  * candidate, keeps the fastest for desc's shape (algorithm, task, classes,
  * log2 rows, log2 features, features tried) for later fits of that shape in
