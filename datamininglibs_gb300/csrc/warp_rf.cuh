@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
   // sorted (key, entry) of the current try; sorted position p at p + p / E, so
   // that lane l's E consecutive positions are read without bank conflicts
   __shared__ unsigned long long s_key[WPB][M + 32];
+  __shared__ int s_hist[WPB][kMaxClasses];  // round scan: class weights of earlier rounds
   const int lane = threadIdx.x & 31;
   const int wb = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -109,6 +110,8 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
     const int m = nd.ecnt;
     const int* ncnt = a.cnt + (long long)node * a.Cmax;
     const int ml = max(1, P.min_leaf);
+    // classification scans by rounds for up to 4 entries a lane
+    constexpr bool kRounds = E <= 4;
     // sort keys: rank << kIdxBits | entry when ranks and entries fit 31 bits
     constexpr int kIdxBits = E == 2 ? 6 : E == 4 ? 7 : E == 8 ? 8 : 9;
     static_assert((1 << kIdxBits) == M, "entry index bits");
@@ -135,11 +138,18 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
 #pragma unroll
     for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
     if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
+    const long long Hn = P.task == 0 ? __ldg(a.H + nd.n) : 0;
+    int wbits;  // bit planes of the node's largest weight
+    {
+      int wm = 1;
+#pragma unroll
+      for (int r = 0; r < E; ++r)
+        if (r * 32 + lane < m) wm = max(wm, s_w[wb][r * 32 + lane]);
+      for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(kFull, wm, o));
+      wbits = 32 - __clz(wm);
+    }
     Cand best;
     best.valid = 0;
-    unsigned long long bestL[CW];
-#pragma unroll
-    for (int j = 0; j < CW; ++j) bestL[j] = 0;
     // the features of tries 0 .. 31, one per lane
     const int fpre = lane < P.n_mand + P.n_opt ? feature_of_try(P, nd, lane) : 0;
     int t = 0;
@@ -175,110 +185,157 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
         for (int r = 0; r < E; ++r) s_key[wb][r * 32 + lane + (r * 32 + lane) / E] = key[r];
       }
       __syncwarp();
-      // boundary scan: lane l owns sorted positions l*E .. l*E+E-1.  One warp
-      // scan of the lanes' row counts and packed class counts (or target
-      // sums), then each lane walks its positions (rolled loops re-reading
-      // shared memory: the class terms are the bulk of the kernel's code).
-      const int p0 = lane * E;
-      const unsigned long long* sk = &s_key[wb][p0 + lane];
-      long long tn = 0, ts = 0;
-      unsigned long long tl[CW];
-#pragma unroll
-      for (int c = 0; c < CW; ++c) tl[c] = 0;
-      unsigned bnd = 0;  // bit j: position p0 + j starts a new key
-      uint32_t prevk =
-          p0 > 0 ? (uint32_t)(s_key[wb][p0 - 1 + (p0 - 1) / E] >> 32) : 0u;
-#pragma unroll 1
-      for (int j = 0; j < E; ++j) {
-        const unsigned long long kv = sk[j];
-        if (kv == ~0ull) break;
-        const int e = (int)(kv & 0xFFFFFFFFull);
-        const uint32_t kk = (uint32_t)(kv >> 32);
-        if (p0 + j > 0 && prevk < kk) bnd |= 1u << j;
-        prevk = kk;
-        const int w = s_w[wb][e];
-        tn += w;
-        if (P.task == 0) {
-          const int k = s_lab[wb][e];
-#pragma unroll
-          for (int c = 0; c < CW; ++c)
-            tl[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
-                     (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
-        } else {
-          ts += s_q[wb][e] * (long long)w;
-        }
-      }
-      long long nl = warp_excl_scan<long long>(tn);
-      long long sl = 0;
-      unsigned long long L[CW];
-      if (P.task == 0) {
-#pragma unroll
-        for (int c = 0; c < CW; ++c) L[c] = warp_excl_scan<unsigned long long>(tl[c]);
-      } else {
-        sl = warp_excl_scan<long long>(ts);
-#pragma unroll
-        for (int c = 0; c < CW; ++c) L[c] = 0;
-      }
-      unsigned long long myL[CW];
-#pragma unroll
-      for (int c = 0; c < CW; ++c) myL[c] = 0;
       long long my_nl = 0, my_sl = 0;
       float bg = -FLT_MAX;
       int bp = -1;
-      NumBest nb;
-      nb.init();
-      long long Q = 0;
-      bool haveQ = false;
+      if (kRounds && P.task == 0) {
+        // round scan (classification, E <= 4): sorted positions r*32 + lane,
+        // one round at a time.  The gain numerator is h(n) - h(nL) - h(nR)
+        // plus the scan of each entry's own-class change: its class weight
+        // below it is that of the earlier rounds (s_hist) plus that of the
+        // lanes below it in its round matching its class (match, bit planes)
+        for (int c = lane; c < C; c += 32) s_hist[wb][c] = 0;
+        __syncwarp();
+        NumBest nb;
+        nb.init();
+        long long carry_n = 0, carry_s = 0;
+        uint32_t lastk = 0;
 #pragma unroll 1
-      for (int j = 0; j < E && bnd >> j; ++j) {
-        const unsigned long long kv = sk[j];
-        const int e = (int)(kv & 0xFFFFFFFFull);
-        const int w = s_w[wb][e];
-        const long long nr = (long long)nd.n - nl;
-        const bool at = ((bnd >> j) & 1u) && nl >= ml && nr >= ml;
-        if (P.task == 0) {
-          const int k = s_lab[wb][e];
-          if (at) {
-            if (!haveQ) {
-              Q = entropy_q_u<2 * CW>(
-                  a.H, C, nl, nr,
-                  [&](int c) {
-                    return (long long)((c & 1) ? (L[c >> 1] >> 32) : (L[c >> 1] & 0xFFFFFFFFull));
-                  },
-                  [&](int c) { return (long long)Nt[c]; });
-              haveQ = true;
-            }
-            if (nb.offer(prior - Q, p0 + j, nd.n)) {
-              my_nl = nl;
-#pragma unroll
-              for (int c = 0; c < CW; ++c) myL[c] = L[c];
-            }
+        for (int r = 0; r < E; ++r) {
+          const int pos = r * 32 + lane;
+          const unsigned long long kv = s_key[wb][pos + pos / E];
+          const bool ok = kv != ~0ull;
+          const int e = (int)(kv & 0xFFFFFFFFull);
+          const uint32_t kk = (uint32_t)(kv >> 32);
+          const int w = ok ? s_w[wb][e] : 0;
+          const int c = ok ? s_lab[wb][e] : -1;
+          const unsigned peers = __match_any_sync(kFull, c);
+          int lw = 0, gw_c = 0;
+          for (int b = 0; b < wbits; ++b) {
+            const unsigned bb = __ballot_sync(kFull, (w >> b) & 1);
+            lw += __popc(bb & peers & lt) << b;
+            gw_c += __popc(bb & peers) << b;
           }
-          if (haveQ && (bnd >> (j + 1)) != 0u) {
-            const long long lc = packed_get<CW>(L, k);
-            Q += entropy_q_move(a.H, nl, nr, lc, (long long)Nt_of<CW>(Nt, k) - lc, w);
+          long long dq = 0;
+          if (ok) {
+            const int L = s_hist[wb][c] + lw;
+            const int R = Nt_of<CW>(Nt, c) - L;
+            dq = (__ldg(a.H + L + w) - __ldg(a.H + L)) + (__ldg(a.H + R - w) - __ldg(a.H + R));
           }
-#pragma unroll
-          for (int c = 0; c < CW; ++c)
-            L[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
-                    (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
-        } else {
-          if (at) {
-            const float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
-            if (bp < 0 || g > bg) {
-              bg = g;
-              bp = p0 + j;
-              my_nl = nl;
-              my_sl = sl;
-            }
-          }
-          sl += s_q[wb][e] * (long long)w;
+          const long long xn = warp_excl_scan<long long>(w);
+          const long long xs = warp_excl_scan<long long>(dq);
+          const long long nl = carry_n + xn, S = carry_s + xs;
+          uint32_t prevk = __shfl_up_sync(kFull, kk, 1);
+          if (lane == 0) prevk = lastk;
+          const long long nr = (long long)nd.n - nl;
+          if (ok && pos > 0 && prevk < kk && nl >= ml && nr >= ml &&
+              nb.offer(Hn - __ldg(a.H + nl) - __ldg(a.H + nr) + S, pos, nd.n))
+            my_nl = nl;
+          carry_n += __shfl_sync(kFull, xn + w, 31);
+          carry_s += __shfl_sync(kFull, xs + dq, 31);
+          lastk = __shfl_sync(kFull, kk, 31);
+          __syncwarp();
+          if (ok && (peers & lt) == 0) s_hist[wb][c] += gw_c;  // one lane per class
+          __syncwarp();
         }
-        nl += w;
-      }
-      if (P.task == 0) {
         bg = nb.gain(nd.n);
         bp = nb.p;
+      } else {
+        // boundary scan: lane l owns sorted positions l*E .. l*E+E-1.  One warp
+        // scan of the lanes' row counts and packed class counts (or target
+        // sums), then each lane walks its positions (rolled loops re-reading
+        // shared memory: the class terms are the bulk of the kernel's code).
+        const int p0 = lane * E;
+        const unsigned long long* sk = &s_key[wb][p0 + lane];
+        long long tn = 0, ts = 0;
+        unsigned long long tl[CW];
+#pragma unroll
+        for (int c = 0; c < CW; ++c) tl[c] = 0;
+        unsigned bnd = 0;  // bit j: position p0 + j starts a new key
+        uint32_t prevk =
+            p0 > 0 ? (uint32_t)(s_key[wb][p0 - 1 + (p0 - 1) / E] >> 32) : 0u;
+#pragma unroll 1
+        for (int j = 0; j < E; ++j) {
+          const unsigned long long kv = sk[j];
+          if (kv == ~0ull) break;
+          const int e = (int)(kv & 0xFFFFFFFFull);
+          const uint32_t kk = (uint32_t)(kv >> 32);
+          if (p0 + j > 0 && prevk < kk) bnd |= 1u << j;
+          prevk = kk;
+          const int w = s_w[wb][e];
+          tn += w;
+          if (P.task == 0) {
+            const int k = s_lab[wb][e];
+#pragma unroll
+            for (int c = 0; c < CW; ++c)
+              tl[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
+                       (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
+          } else {
+            ts += s_q[wb][e] * (long long)w;
+          }
+        }
+        long long nl = warp_excl_scan<long long>(tn);
+        long long sl = 0;
+        unsigned long long L[CW];
+        if (P.task == 0) {
+#pragma unroll
+          for (int c = 0; c < CW; ++c) L[c] = warp_excl_scan<unsigned long long>(tl[c]);
+        } else {
+          sl = warp_excl_scan<long long>(ts);
+#pragma unroll
+          for (int c = 0; c < CW; ++c) L[c] = 0;
+        }
+        NumBest nb;
+        nb.init();
+        long long Q = 0;
+        bool haveQ = false;
+#pragma unroll 1
+        for (int j = 0; j < E && bnd >> j; ++j) {
+          const unsigned long long kv = sk[j];
+          const int e = (int)(kv & 0xFFFFFFFFull);
+          const int w = s_w[wb][e];
+          const long long nr = (long long)nd.n - nl;
+          const bool at = ((bnd >> j) & 1u) && nl >= ml && nr >= ml;
+          if (P.task == 0) {
+            const int k = s_lab[wb][e];
+            if (at) {
+              if (!haveQ) {
+                Q = entropy_q_u<2 * CW>(
+                    a.H, C, nl, nr,
+                    [&](int c) {
+                      return (long long)((c & 1) ? (L[c >> 1] >> 32) : (L[c >> 1] & 0xFFFFFFFFull));
+                    },
+                    [&](int c) { return (long long)Nt[c]; });
+                haveQ = true;
+              }
+              if (nb.offer(prior - Q, p0 + j, nd.n)) my_nl = nl;
+            }
+            if (haveQ && (bnd >> (j + 1)) != 0u) {
+              const long long lc = packed_get<CW>(L, k);
+              Q += entropy_q_move(a.H, nl, nr, lc, (long long)Nt_of<CW>(Nt, k) - lc, w);
+            }
+#pragma unroll
+            for (int c = 0; c < CW; ++c)
+              L[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
+                      (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
+          } else {
+            if (at) {
+              const float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
+              if (bp < 0 || g > bg) {
+                bg = g;
+                bp = p0 + j;
+                my_nl = nl;
+                my_sl = sl;
+              }
+            }
+            sl += s_q[wb][e] * (long long)w;
+          }
+          nl += w;
+        }
+        if (P.task == 0) {
+          bg = nb.gain(nd.n);
+          bp = nb.p;
+        }
       }
       // warp argmax: higher gain, then lower position
       float wg = bg;
@@ -295,7 +352,6 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
       }
       Cand cd;
       cd.f = f;
-      unsigned long long candL[CW];
       if (wp >= 0) {
         const int src = __ffs(__ballot_sync(kFull, bp == wp)) - 1;
         cd.valid = 1;
@@ -309,31 +365,20 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
         cd.nl_e = wp;
         cd.nl = (int)__shfl_sync(kFull, my_nl, src);
         cd.suml = __shfl_sync(kFull, my_sl, src);
-#pragma unroll
-        for (int j = 0; j < CW; ++j) candL[j] = __shfl_sync(kFull, myL[j], src);
       } else {
         cd.valid = 0;
         cd.gain = -FLT_MAX;
         cd.thr = 0.0f;
         cd.nl_e = cd.nl = 0;
         cd.suml = 0;
-#pragma unroll
-        for (int j = 0; j < CW; ++j) candL[j] = 0;
       }
       bool more;
-      bool take;
       if (t < P.n_mand) {
-        take = (t == 0 || better(cd, best));
-        if (take) best = cd;
+        if (t == 0 || better(cd, best)) best = cd;
         more = (t + 1 < P.n_mand) || (P.n_opt > 0 && !(best.valid && best.gain >= kSensible));
       } else {
-        take = better(cd, best);
-        if (take) best = cd;
+        if (better(cd, best)) best = cd;
         more = !(cd.valid && cd.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
-      }
-      if (take) {
-#pragma unroll
-        for (int j = 0; j < CW; ++j) bestL[j] = candL[j];
       }
       __syncwarp();
       if (!more) break;
@@ -348,15 +393,25 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
       continue;
     }
     if (lane == 0) write_result(a.res, a.res_cnt, a.Cmax, node, best, nullptr, 0);
-    if (P.task == 0 && lane < C) a.res_cnt[(long long)node * a.Cmax + lane] = (int)packed_get<CW>(bestL, lane);
-    // stable partition, 32 entries per round
+    // stable partition, 32 entries per round; the left class counts of the
+    // split (packed two per word) from the entries that go left
     const float* xb = P.X + (long long)best.f * P.N;
     int offl = 0, offr = 0;
+    unsigned long long lcnt[CW];
+#pragma unroll
+    for (int c = 0; c < CW; ++c) lcnt[c] = 0;
 #pragma unroll
     for (int r = 0; r < E; ++r) {
       const int i = r * 32 + lane;
       const bool valid = i < m;
       const bool left = valid && goes_left(__ldg(xb + rowr[r]), best.thr);
+      if (P.task == 0 && left) {
+        const int k = s_lab[wb][i];
+        const unsigned long long w = (unsigned long long)s_w[wb][i];
+#pragma unroll
+        for (int c = 0; c < CW; ++c)
+          lcnt[c] += (k == 2 * c ? w : 0ull) | (k == 2 * c + 1 ? (w << 32) : 0ull);
+      }
       const unsigned lm = __ballot_sync(kFull, left);
       const unsigned vm = __ballot_sync(kFull, valid);
       if (valid) {
@@ -368,6 +423,11 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
       }
       offl += __popc(lm);
       offr += __popc(vm) - __popc(lm);
+    }
+    if (P.task == 0) {
+#pragma unroll
+      for (int c = 0; c < CW; ++c) lcnt[c] = warp_sum<unsigned long long>(lcnt[c]);
+      if (lane < C) a.res_cnt[(long long)node * a.Cmax + lane] = (int)packed_get<CW>(lcnt, lane);
     }
     __syncwarp();
   }
