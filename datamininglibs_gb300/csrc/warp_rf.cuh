@@ -2,11 +2,16 @@
 //
 // The node's (key, entry) pairs are held striped in registers (element
 // r*32 + lane in register r), sorted by a bitonic network (register
-// compare-exchanges for distances >= 32, shuffles below), then scanned 32
-// consecutive elements at a time with warp scans of the packed class counts
-// (two 32-bit counts per 64-bit word) or of the regression count / sum.  No
-// block barriers; eight nodes per 256-thread block.  Same candidate rules as
-// the CTA kernels (lib_ensembles/source/gpurf.cu:131-259, 618-917 restated).
+// compare-exchanges for distances >= 32, shuffles below) and written to shared
+// memory.  Classification scans the sorted positions one round of 32 at a
+// time: each entry's class weight below it (earlier rounds from a per-warp
+// class histogram, its round from a match instruction and the weights' bit
+// planes) gives the change its move to the left side makes to the entropy
+// sum, and one warp scan of those changes gives every boundary's exact gain
+// numerator.  Regression scans E consecutive positions per lane after one
+// warp scan of counts and target sums.  No block barriers; a node per warp,
+// eight warps a block (two for 512-entry nodes).  Same candidate rules as the CTA kernels
+// (lib_ensembles/source/gpurf.cu:131-259, 618-917 restated).
 #pragma once
 #include "fit_kernels.cuh"
 
@@ -110,8 +115,6 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
     const int m = nd.ecnt;
     const int* ncnt = a.cnt + (long long)node * a.Cmax;
     const int ml = max(1, P.min_leaf);
-    // classification scans by rounds for up to 4 entries a lane
-    constexpr bool kRounds = E <= 4;
     // sort keys: rank << kIdxBits | entry when ranks and entries fit 31 bits
     constexpr int kIdxBits = E == 2 ? 6 : E == 4 ? 7 : E == 8 ? 8 : 9;
     static_assert((1 << kIdxBits) == M, "entry index bits");
@@ -133,11 +136,9 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
       }
     }
     __syncwarp();
-    long long prior = 0;
     int Nt[2 * CW];
 #pragma unroll
     for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
-    if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     const long long Hn = P.task == 0 ? __ldg(a.H + nd.n) : 0;
     int wbits;  // bit planes of the node's largest weight
     {
@@ -188,8 +189,8 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
       long long my_nl = 0, my_sl = 0;
       float bg = -FLT_MAX;
       int bp = -1;
-      if (kRounds && P.task == 0) {
-        // round scan (classification, E <= 4): sorted positions r*32 + lane,
+      if (P.task == 0) {
+        // classification, by rounds: sorted positions r*32 + lane,
         // one round at a time.  The gain numerator is h(n) - h(nL) - h(nR)
         // plus the scan of each entry's own-class change: its class weight
         // below it is that of the earlier rounds (s_hist) plus that of the
@@ -241,16 +242,12 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
         bg = nb.gain(nd.n);
         bp = nb.p;
       } else {
-        // boundary scan: lane l owns sorted positions l*E .. l*E+E-1.  One warp
-        // scan of the lanes' row counts and packed class counts (or target
-        // sums), then each lane walks its positions (rolled loops re-reading
-        // shared memory: the class terms are the bulk of the kernel's code).
+        // regression: lane l owns sorted positions l*E .. l*E+E-1; one warp
+        // scan of the lanes' row counts and target sums, then each lane walks
+        // its positions (rolled loops re-reading shared memory)
         const int p0 = lane * E;
         const unsigned long long* sk = &s_key[wb][p0 + lane];
         long long tn = 0, ts = 0;
-        unsigned long long tl[CW];
-#pragma unroll
-        for (int c = 0; c < CW; ++c) tl[c] = 0;
         unsigned bnd = 0;  // bit j: position p0 + j starts a new key
         uint32_t prevk =
             p0 > 0 ? (uint32_t)(s_key[wb][p0 - 1 + (p0 - 1) / E] >> 32) : 0u;
@@ -264,77 +261,27 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
           prevk = kk;
           const int w = s_w[wb][e];
           tn += w;
-          if (P.task == 0) {
-            const int k = s_lab[wb][e];
-#pragma unroll
-            for (int c = 0; c < CW; ++c)
-              tl[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
-                       (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
-          } else {
-            ts += s_q[wb][e] * (long long)w;
-          }
+          ts += s_q[wb][e] * (long long)w;
         }
         long long nl = warp_excl_scan<long long>(tn);
-        long long sl = 0;
-        unsigned long long L[CW];
-        if (P.task == 0) {
-#pragma unroll
-          for (int c = 0; c < CW; ++c) L[c] = warp_excl_scan<unsigned long long>(tl[c]);
-        } else {
-          sl = warp_excl_scan<long long>(ts);
-#pragma unroll
-          for (int c = 0; c < CW; ++c) L[c] = 0;
-        }
-        NumBest nb;
-        nb.init();
-        long long Q = 0;
-        bool haveQ = false;
+        long long sl = warp_excl_scan<long long>(ts);
 #pragma unroll 1
         for (int j = 0; j < E && bnd >> j; ++j) {
           const unsigned long long kv = sk[j];
           const int e = (int)(kv & 0xFFFFFFFFull);
           const int w = s_w[wb][e];
           const long long nr = (long long)nd.n - nl;
-          const bool at = ((bnd >> j) & 1u) && nl >= ml && nr >= ml;
-          if (P.task == 0) {
-            const int k = s_lab[wb][e];
-            if (at) {
-              if (!haveQ) {
-                Q = entropy_q_u<2 * CW>(
-                    a.H, C, nl, nr,
-                    [&](int c) {
-                      return (long long)((c & 1) ? (L[c >> 1] >> 32) : (L[c >> 1] & 0xFFFFFFFFull));
-                    },
-                    [&](int c) { return (long long)Nt[c]; });
-                haveQ = true;
-              }
-              if (nb.offer(prior - Q, p0 + j, nd.n)) my_nl = nl;
+          if (((bnd >> j) & 1u) && nl >= ml && nr >= ml) {
+            const float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
+            if (bp < 0 || g > bg) {
+              bg = g;
+              bp = p0 + j;
+              my_nl = nl;
+              my_sl = sl;
             }
-            if (haveQ && (bnd >> (j + 1)) != 0u) {
-              const long long lc = packed_get<CW>(L, k);
-              Q += entropy_q_move(a.H, nl, nr, lc, (long long)Nt_of<CW>(Nt, k) - lc, w);
-            }
-#pragma unroll
-            for (int c = 0; c < CW; ++c)
-              L[c] += (k == 2 * c ? (unsigned long long)w : 0ull) |
-                      (k == 2 * c + 1 ? ((unsigned long long)w << 32) : 0ull);
-          } else {
-            if (at) {
-              const float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
-              if (bp < 0 || g > bg) {
-                bg = g;
-                bp = p0 + j;
-                my_nl = nl;
-                my_sl = sl;
-              }
-            }
-            sl += s_q[wb][e] * (long long)w;
           }
+          sl += s_q[wb][e] * (long long)w;
           nl += w;
-        }
-        if (P.task == 0) {
-          bg = nb.gain(nd.n);
-          bp = nb.p;
         }
       }
       // warp argmax: higher gain, then lower position
