@@ -431,7 +431,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     int* rowsB = (int*)alloc(sizeof(int) * total_slots);
     int* wA = any_weights ? (int*)alloc(sizeof(int) * total_slots) : nullptr;
     int* wB = any_weights ? (int*)alloc(sizeof(int) * total_slots) : nullptr;
-    uint2* scratch = any_weights ? (uint2*)alloc(sizeof(uint2) * 2 * total_slots) : nullptr;
+    // bootstrap multiplicities per entry slot, read by k_roots
+    int* boot = any_weights ? (int*)alloc(sizeof(int) * total_slots) : nullptr;
     // big-node scratch: 4 words per entry of the largest RF tree, per CTA
     int max_mand = 1, max_opt = 0;
     long long slot_stride = 0;
@@ -509,16 +510,16 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       return Q;
     };
     if (any_weights) {
-      DML_CK(cudaMemsetAsync(scratch, 0, sizeof(int) * total_slots, s));
+      DML_CK(cudaMemsetAsync(boot, 0, sizeof(int) * total_slots, s));
       long long maxN = 0;
       for (auto& P : hp) maxN = std::max(maxN, P.N);
       const int chunk = 1 << 16;
       dim3 g((unsigned)((maxN + chunk - 1) / chunk), (unsigned)total_trees);
-      k_boot_count<<<g, 256, 0, s>>>(d_probs, d_tree_prob, (int*)scratch, chunk);
+      k_boot_count<<<g, 256, 0, s>>>(d_probs, d_tree_prob, boot, chunk);
       DML_CK(cudaGetLastError());
       ++st.launches;
     }
-    k_roots<1024><<<total_trees, 1024, 0, s>>>(d_probs, d_tree_prob, (const int*)scratch, rowsA,
+    k_roots<1024><<<total_trees, 1024, 0, s>>>(d_probs, d_tree_prob, boot, rowsA,
                                                wA, cur.p, cnt_cur.p, Cmax, res_cur.p, queues(),
                                                d_stats);
     DML_CK(cudaGetLastError());
@@ -554,8 +555,6 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       a.wA = wA;
       a.rowsB = rowsB;
       a.wB = wB;
-      a.scratch = scratch;
-      a.scratch_half = total_slots;
       a.H = H;
       a.stats = d_stats;
       a.smem_cap = tune.smem_cap;
@@ -1149,8 +1148,6 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
       a.wA = wA;
       a.rowsB = rowsB;
       a.wB = wB;
-      a.scratch = nullptr;  // every node of <= kNaMaxRows entries sorts in shared memory
-      a.scratch_half = 0;
       a.H = H;
       a.stats = d_stats;
       a.smem_cap = kSmemCap;

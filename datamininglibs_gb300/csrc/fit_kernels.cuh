@@ -261,8 +261,6 @@ struct LevelArgs {
   const int* wA;        // null for unit weights (ERT)
   int* rowsB;
   int* wB;
-  uint2* scratch;       // two pair buffers per entry slot: scratch[slot], scratch[slot + total]
-  long long scratch_half;
   const long long* H;   // n*ln(n) table, fixed point 2^-28
   long long* stats;     // [2] += tries evaluated x node entries, [3] += node entries
   int smem_cap;         // entries per node of the shared-memory RF search's buffers
@@ -453,10 +451,9 @@ __global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
 }
 
 // ============================================================ RF (CTA, sorted)
-// Radix sort (LSD, 8-bit digits) of (key, value) pairs held in shared memory
-// or, for large nodes, in global scratch processed tile by tile.  Stability
-// comes from per-warp contiguous chunks and in-order ranking of equal digits
-// within a warp (digit_peers).
+// Radix sort (LSD, 8-bit digits) of (key, value) pairs held in shared memory.
+// Stability comes from per-warp contiguous chunks and in-order ranking of
+// equal digits within a warp (digit_peers).
 // Lanes of `mask` whose digit equals this lane's.  Every lane of `mask` must
 // call it.  (One match instruction measured faster on the big-node passes than
 // eight ballots, one per digit bit.)
@@ -547,327 +544,6 @@ __device__ bool cta_radix_sort_diff(uint32_t* k, uint32_t* v, uint32_t* k2, uint
     in_primary = !in_primary;
   }
   return !in_primary;
-}
-
-// Sorts pairs in place (result back in k/v).  Passes whose digit is constant
-// across all keys are skipped.
-template <int BLOCK>
-__device__ void cta_radix_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2, int m,
-                               SortSmem<BLOCK>& S, unsigned* red) {
-  // OR / AND of all keys
-  unsigned o = 0, an = 0xFFFFFFFFu;
-  for (int i = threadIdx.x; i < m; i += BLOCK) {
-    o |= k[i];
-    an &= k[i];
-  }
-  for (int s = 16; s > 0; s >>= 1) {
-    o |= __shfl_xor_sync(kFull, o, s);
-    an &= __shfl_xor_sync(kFull, an, s);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    red[2 * (threadIdx.x >> 5)] = o;
-    red[2 * (threadIdx.x >> 5) + 1] = an;
-  }
-  __syncthreads();
-  unsigned diff = 0;
-  {
-    unsigned oo = 0, aa = 0xFFFFFFFFu;
-    for (int w = 0; w < BLOCK / 32; ++w) {
-      oo |= red[2 * w];
-      aa &= red[2 * w + 1];
-    }
-    diff = oo ^ aa;
-  }
-  __syncthreads();
-  bool in_primary = true;
-  for (int shift = 0; shift < 32; shift += 8) {
-    if (((diff >> shift) & 255u) == 0) continue;
-    if (in_primary)
-      radix_pass<BLOCK>(k, v, k2, v2, m, shift, S);
-    else
-      radix_pass<BLOCK>(k2, v2, k, v, m, shift, S);
-    in_primary = !in_primary;
-  }
-  if (!in_primary) {
-    for (int i = threadIdx.x; i < m; i += BLOCK) {
-      k[i] = k2[i];
-      v[i] = v2[i];
-    }
-    __syncthreads();
-  }
-}
-
-// Best boundary of sorted pairs: classification with packed 2 x 32-bit class
-// prefix counts (CW = ceil(C/2) words), or regression with count / sum scans.
-// Writes the try's candidate and (classification) the left class counts of
-// the chosen boundary into candL.
-template <int BLOCK, int CW>
-__device__ void cta_best_boundary(const uint32_t* sk, const uint32_t* sv, int m, const LNode& nd,
-                                  const ProbDesc& P, const int* ncnt, const int* lw_lab,
-                                  const int* lw_w, const long long* vq, const long long* H,
-                                  long long prior, Cand* cand, int* candL, int f, const float* xf,
-                                  const int* rows, unsigned long long* sm64, int* sm_bestpos,
-                                  float* sm_bestg, unsigned long long* carry) {
-  const int C = P.C;
-  const int ml = max(1, P.min_leaf);
-  float my_g = -FLT_MAX;
-  int my_p = -1;
-  unsigned long long myL[CW > 0 ? CW : 1];
-  long long my_nl = 0, my_sl = 0;
-  if (threadIdx.x < 2 * CW + 2) carry[threadIdx.x] = 0;
-  __syncthreads();
-  for (int base = 0; base < m; base += BLOCK) {
-    const int p = base + threadIdx.x;
-    const bool act = p < m;
-    const int e = act ? (int)sv[p] : 0;
-    const int w = act ? (lw_w ? lw_w[e] : 1) : 0;
-    if (P.task == 0) {
-      const int k = act ? lw_lab[e] : -1;
-      unsigned long long L[CW > 0 ? CW : 1];
-      long long nl = 0;
-#pragma unroll
-      for (int j = 0; j < CW; ++j) {
-        unsigned long long v = (k == 2 * j ? (unsigned long long)w : 0ull) |
-                               (k == 2 * j + 1 ? ((unsigned long long)w << 32) : 0ull);
-        unsigned long long tot;
-        unsigned long long ex = block_excl_scan<BLOCK, unsigned long long>(v, &tot, sm64);
-        L[j] = ex + carry[j];
-        nl += (long long)(L[j] & 0xFFFFFFFFull) + (long long)(L[j] >> 32);
-        __syncthreads();
-        if (threadIdx.x == 0) carry[j] += tot;
-      }
-      __syncthreads();
-      if (act && p > 0 && sk[p - 1] < sk[p]) {
-        long long nr = (long long)nd.n - nl;
-        if (nl >= ml && nr >= ml) {
-          float g = entropy_gain(
-              H, prior, C, nl, nr,
-              [&](int c) {
-                unsigned long long x = L[0];
-#pragma unroll
-                for (int j = 1; j < CW; ++j)
-                  if ((c >> 1) == j) x = L[j];
-                return (long long)((c & 1) ? (x >> 32) : (x & 0xFFFFFFFFull));
-              },
-              [&](int c) { return (long long)ncnt[c]; });
-          if (my_p < 0 || g > my_g) {
-            my_g = g;
-            my_p = p;
-#pragma unroll
-            for (int j = 0; j < CW; ++j) myL[j] = L[j];
-            my_nl = nl;
-          }
-        }
-      }
-    } else {
-      const long long qw = act ? vq[e] * (long long)w : 0;
-      unsigned long long totn, tots;
-      long long exn = (long long)block_excl_scan<BLOCK, unsigned long long>(
-          (unsigned long long)w, &totn, sm64);
-      long long nl = exn + (long long)carry[0];
-      long long exs = (long long)block_excl_scan<BLOCK, unsigned long long>(
-          (unsigned long long)qw, &tots, sm64);
-      long long sl = exs + (long long)carry[1];
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        carry[0] += totn;
-        carry[1] += tots;
-      }
-      __syncthreads();
-      if (act && p > 0 && sk[p - 1] < sk[p]) {
-        long long nr = (long long)nd.n - nl;
-        if (nl >= ml && nr >= ml) {
-          float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
-          if (my_p < 0 || g > my_g) {
-            my_g = g;
-            my_p = p;
-            my_nl = nl;
-            my_sl = sl;
-          }
-        }
-      }
-    }
-  }
-  // block argmax: higher gain, then lower position
-  sm_bestg[threadIdx.x] = my_g;
-  sm_bestpos[threadIdx.x] = my_p;
-  __syncthreads();
-  for (int s = BLOCK / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      float g2 = sm_bestg[threadIdx.x + s];
-      int p2 = sm_bestpos[threadIdx.x + s];
-      float g1 = sm_bestg[threadIdx.x];
-      int p1 = sm_bestpos[threadIdx.x];
-      bool take = p2 >= 0 && (p1 < 0 || g2 > g1 || (g2 == g1 && p2 < p1));
-      if (take) {
-        sm_bestg[threadIdx.x] = g2;
-        sm_bestpos[threadIdx.x] = p2;
-      }
-    }
-    __syncthreads();
-  }
-  const int bp = sm_bestpos[0];
-  if (bp >= 0 && my_p == bp) {  // the winning thread publishes its prefix
-    Cand c;
-    c.valid = 1;
-    c.gain = my_g;
-    c.f = f;
-    float xa = __ldg(xf + rows[sv[bp - 1]]);
-    float xb = __ldg(xf + rows[sv[bp]]);
-    c.thr = midpoint_threshold(xa, xb);
-    c.nl_e = bp;
-    c.nl = (int)my_nl;
-    c.suml = my_sl;
-    *cand = c;
-    if (P.task == 0)
-      for (int cc = 0; cc < C; ++cc) {
-        unsigned long long x = myL[0];
-#pragma unroll
-        for (int j = 1; j < CW; ++j)
-          if ((cc >> 1) == j) x = myL[j];
-        candL[cc] = (int)((cc & 1) ? (x >> 32) : (x & 0xFFFFFFFFull));
-      }
-  }
-  if (bp < 0 && threadIdx.x == 0) {
-    Cand c;
-    c.valid = 0;
-    c.gain = -FLT_MAX;
-    c.f = f;
-    c.thr = 0.0f;
-    c.nl_e = 0;
-    c.nl = 0;
-    c.suml = 0;
-    *cand = c;
-  }
-  __syncthreads();
-}
-
-// RF node in a CTA.  SMEM_CAP: nodes with at most that many entries are
-// sorted in shared memory; larger ones use the node's own slots of the other
-// entry buffer and the scratch buffer as tile-sorted global storage.
-template <int BLOCK, int CW, int SMEM_CAP>
-__global__ void __launch_bounds__(BLOCK) k_rf_cta(LevelArgs a, int big) {
-  __shared__ SortSmem<BLOCK> S;
-  __shared__ unsigned long long sm64[BLOCK / 32];
-  __shared__ unsigned red[2 * (BLOCK / 32)];
-  __shared__ int sm_bestpos[BLOCK];
-  __shared__ float sm_bestg[BLOCK];
-  __shared__ unsigned long long carry[2 * 16 + 2];
-  __shared__ Cand s_cand, s_best;
-  __shared__ int s_candL[kMaxClasses], s_bestL[kMaxClasses];
-  __shared__ long long s_prior;
-  __shared__ int s_scan[BLOCK / 32];
-  __shared__ int s_next;
-  extern __shared__ __align__(16) unsigned char dsm[];
-  for (int wi = blockIdx.x; wi < a.nwork; wi += gridDim.x) {
-    const int node = a.work[wi];
-    const LNode nd = a.nodes[node];
-    const ProbDesc& P = a.probs[nd.prob];
-    const int C = P.C;
-    const int m = nd.ecnt;
-    const int* rows = a.rowsA + nd.ebeg;
-    const int* wts = a.wA ? a.wA + nd.ebeg : nullptr;
-    const int* ncnt = a.cnt + (long long)node * a.Cmax;
-    // per-entry labels / targets, keys and values
-    uint32_t *k1, *v1, *k2, *v2;
-    int* lab_e = nullptr;
-    long long* q_e = nullptr;
-    if (!big) {
-      uint32_t* base = (uint32_t*)dsm;
-      k1 = base;
-      v1 = base + SMEM_CAP;
-      k2 = base + 2 * SMEM_CAP;
-      v2 = base + 3 * SMEM_CAP;
-      if (P.task == 0)
-        lab_e = (int*)(base + 4 * SMEM_CAP);
-      else
-        q_e = (long long*)(base + 4 * SMEM_CAP);
-      for (int i = threadIdx.x; i < m; i += BLOCK) {
-        int row = __ldg(rows + i);
-        if (P.task == 0)
-          lab_e[i] = __ldg(P.lab + row);
-        else
-          q_e[i] = __ldg(P.q + row);
-      }
-    } else {
-      // pairs: (rowsB, wB) slots of the node as one uint2-sized buffer is not
-      // available separately, so the scratch holds both ping-pong buffers
-      uint2* sc = a.scratch;
-      k1 = (uint32_t*)(sc + nd.ebeg);
-      v1 = k1 + m;
-      k2 = (uint32_t*)(sc + a.scratch_half + nd.ebeg);
-      v2 = k2 + m;
-    }
-    if (threadIdx.x == 0 && P.task == 0)
-      s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
-    __syncthreads();
-    int t = 0;
-    bool stop = false;
-    while (!stop) {
-      const int f = feature_of_try(P, nd, t);
-      const float* xf = P.X + (long long)f * P.N;
-      for (int i = threadIdx.x; i < m; i += BLOCK) {
-        k1[i] = orderable(__ldg(xf + __ldg(rows + i)));
-        v1[i] = (uint32_t)i;
-      }
-      __syncthreads();
-      cta_radix_sort<BLOCK>(k1, v1, k2, v2, m, S, red);
-      // labels / targets: smem copies for small nodes, gathers for big ones
-      if (!big) {
-        cta_best_boundary<BLOCK, CW>(k1, v1, m, nd, P, ncnt, lab_e, wts, q_e, a.H, s_prior,
-                                     &s_cand, s_candL, f, xf, rows, sm64, sm_bestpos, sm_bestg,
-                                     carry);
-      } else {
-        // gather labels/targets by entry index from global memory: stage the
-        // per-entry values in the second pair buffer (no longer needed)
-        if (P.task == 0) {
-          int* le = (int*)k2;
-          for (int i = threadIdx.x; i < m; i += BLOCK) le[i] = __ldg(P.lab + __ldg(rows + i));
-          __syncthreads();
-          cta_best_boundary<BLOCK, CW>(k1, v1, m, nd, P, ncnt, le, wts, nullptr, a.H, s_prior,
-                                       &s_cand, s_candL, f, xf, rows, sm64, sm_bestpos,
-                                       sm_bestg, carry);
-        } else {
-          long long* qe = (long long*)k2;  // k2,v2 contiguous: 8 bytes per entry
-          for (int i = threadIdx.x; i < m; i += BLOCK) qe[i] = __ldg(P.q + __ldg(rows + i));
-          __syncthreads();
-          cta_best_boundary<BLOCK, CW>(k1, v1, m, nd, P, ncnt, nullptr, wts, qe, a.H, s_prior,
-                                       &s_cand, s_candL, f, xf, rows, sm64, sm_bestpos,
-                                       sm_bestg, carry);
-        }
-      }
-      if (threadIdx.x == 0) {
-        const bool mand = t < P.n_mand;
-        if (t == 0 || better(s_cand, s_best)) {
-          s_best = s_cand;
-          if (P.task == 0)
-            for (int c = 0; c < C; ++c) s_bestL[c] = s_candL[c];
-        }
-        bool next;
-        if (mand)
-          next = (t + 1 < P.n_mand) ||
-                 (P.n_opt > 0 && !(s_best.valid && s_best.gain >= kSensible));
-        else
-          next = !(s_cand.valid && s_cand.gain >= kSensible) && (t + 1 < P.n_mand + P.n_opt);
-        s_next = next ? 1 : 0;
-      }
-      __syncthreads();
-      stop = s_next == 0;
-      __syncthreads();
-      ++t;
-    }
-    const Cand b = s_best;
-    if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.stats[2], (unsigned long long)t * m);
-    if (!b.valid) {
-      if (threadIdx.x == 0) write_leaf(a.res, node);
-    } else {
-      if (threadIdx.x == 0)
-        write_result(a.res, a.res_cnt, a.Cmax, node, b, P.task == 0 ? s_bestL : nullptr, C);
-      cta_partition<BLOCK>(a.rowsA, a.wA, a.rowsB, a.wB, nd.ebeg, m, b.nl_e,
-                           P.X + (long long)b.f * P.N, b.thr, s_scan);
-    }
-    __syncthreads();
-  }
 }
 
 }  // namespace dml
