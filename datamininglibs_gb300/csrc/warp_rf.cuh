@@ -83,7 +83,8 @@ constexpr int warp_rf_wpb() {
   return E >= 16 ? 2 : 8;
 }
 
-// At most 128 registers a thread: 16 warps of an SM.
+// Resident blocks per SM the registers are sized for: 16 warps (128 registers
+// a thread; a 512-entry block's 25 KB of shared memory also allows eight).
 template <int E>
 constexpr int warp_rf_min_blocks() {
   return 16 / warp_rf_wpb<E>();
@@ -96,8 +97,10 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
   constexpr int WPB = warp_rf_wpb<E>();
   __shared__ int s_row[WPB][M];
   __shared__ int s_w[WPB][M];
-  __shared__ int s_lab[WPB][M];
-  __shared__ long long s_q[WPB][M];
+  // labels (classification) or fixed-point targets (regression) of the entries
+  __shared__ long long s_lq[WPB][M];
+  int* const s_lab_w = reinterpret_cast<int*>(s_lq[threadIdx.x >> 5]);
+  const long long* const s_q_w = s_lq[threadIdx.x >> 5];
   // sorted (key, entry) of the current try; sorted position p at p + p / E, so
   // that lane l's E consecutive positions are read without bank conflicts
   __shared__ unsigned long long s_key[WPB][M + 32];
@@ -130,9 +133,9 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
         s_row[wb][i] = row;
         s_w[wb][i] = a.wA ? __ldg(a.wA + nd.ebeg + i) : 1;
         if (P.task == 0)
-          s_lab[wb][i] = __ldg(P.lab + row);
+          s_lab_w[i] = __ldg(P.lab + row);
         else
-          s_q[wb][i] = __ldg(P.q + row);
+          s_lq[wb][i] = __ldg(P.q + row);
       }
     }
     __syncwarp();
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
           const int e = (int)(kv & 0xFFFFFFFFull);
           const uint32_t kk = (uint32_t)(kv >> 32);
           const int w = ok ? s_w[wb][e] : 0;
-          const int c = ok ? s_lab[wb][e] : -1;
+          const int c = ok ? s_lab_w[e] : -1;
           const unsigned peers = __match_any_sync(kFull, c);
           int lw = 0, gw_c = 0;
           for (int b = 0; b < wbits; ++b) {
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
           prevk = kk;
           const int w = s_w[wb][e];
           tn += w;
-          ts += s_q[wb][e] * (long long)w;
+          ts += s_q_w[e] * (long long)w;
         }
         long long nl = warp_excl_scan<long long>(tn);
         long long sl = warp_excl_scan<long long>(ts);
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
               my_sl = sl;
             }
           }
-          sl += s_q[wb][e] * (long long)w;
+          sl += s_q_w[e] * (long long)w;
           nl += w;
         }
       }
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
       const bool valid = i < m;
       const bool left = valid && goes_left(__ldg(xb + rowr[r]), best.thr);
       if (P.task == 0 && left) {
-        const int k = s_lab[wb][i];
+        const int k = s_lab_w[i];
         const unsigned long long w = (unsigned long long)s_w[wb][i];
 #pragma unroll
         for (int c = 0; c < CW; ++c)
