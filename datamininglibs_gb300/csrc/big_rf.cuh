@@ -507,7 +507,11 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
           o |= k;
           an &= k;
         }
-        for (int d = 0; d < nbytes; ++d) hist_add_round(S.dh[d], (k >> (8 * d)) & 255u, act);
+        // lower bytes vary across the node's keys: plain atomics; the top byte
+        // may be one value for the whole round (one atomic for the round)
+        for (int d = 0; d + 1 < nbytes; ++d)
+          if (act) atomicAdd(&S.dh[d][(k >> (8 * d)) & 255u], 1u);
+        hist_add_round(S.dh[nbytes - 1], (k >> (8 * (nbytes - 1))) & 255u, act);
       }
     }
 #pragma unroll
