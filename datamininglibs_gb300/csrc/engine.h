@@ -2,12 +2,22 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
 
 #include "../../include/dml.h"
 #include "dml_internal.h"
+
+namespace dml {
+// One device allocation holding the models of every forest of a fit; each
+// forest holds a reference, the last free releases it.
+struct ForestBlock {
+  void* base = nullptr;
+  std::atomic<int> refs{0};
+};
+}  // namespace dml
 
 struct dml_forest {
   int task = 0, n_trees = 0, n_classes = 1, n_features = 0;
@@ -16,6 +26,7 @@ struct dml_forest {
   float* probs = nullptr;              // device
   long long n_probs = 0;
   dml::PNode* pnodes = nullptr;        // device, predict layout
+  dml::ForestBlock* block = nullptr;   // set when the three arrays live in a shared block
   int max_depth = 0;
   double fit_ms = 0.0;
   int device = 0;

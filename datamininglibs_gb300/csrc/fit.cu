@@ -765,6 +765,21 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       DML_CK(cudaMemcpyAsync(hseg.data(), segs.p, sizeof(Seg) * hseg.size(),
                              cudaMemcpyDeviceToHost, s));
     DML_CK(cudaStreamSynchronize(s));
+    // one block for every forest's node, probability and predict arrays
+    auto al = [](long long b) { return (b + 255) & ~255ll; };
+    long long block_bytes = 0;
+    for (int i = 0; i < nprob; ++i)
+      block_bytes += al(sizeof(ClassifyNode) * std::max<long long>(1, fnodes[i])) +
+                     al(sizeof(float) * std::max<long long>(1, fleaves[i] * hp[i].C)) +
+                     al(sizeof(PNode) * std::max<long long>(1, fnodes[i]));
+    ForestBlock* block = new ForestBlock();
+    if (cudaMalloc(&block->base, block_bytes) != cudaSuccess) {
+      delete block;
+      cudaGetLastError();
+      set_error("device allocation of %lld bytes for the forests failed", block_bytes);
+      throw CudaError{cudaErrorMemoryAllocation};
+    }
+    char* bp = (char*)block->base;
     std::vector<GatherSeg> gsegs;
     for (int i = 0; i < nprob; ++i) {
       dml_forest* f = new dml_forest();
@@ -777,8 +792,14 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       f->n_probs = fleaves[i] * hp[i].C;
       f->fit_ms = loop_ms;
       cudaGetDevice(&f->device);
-      DML_CK(cudaMalloc(&f->nodes, sizeof(ClassifyNode) * std::max<long long>(1, f->n_nodes)));
-      DML_CK(cudaMalloc(&f->probs, sizeof(float) * std::max<long long>(1, f->n_probs)));
+      f->block = block;
+      block->refs.fetch_add(1);
+      f->nodes = (ClassifyNode*)bp;
+      bp += al(sizeof(ClassifyNode) * std::max<long long>(1, f->n_nodes));
+      f->probs = (float*)bp;
+      bp += al(sizeof(float) * std::max<long long>(1, f->n_probs));
+      f->pnodes = (PNode*)bp;
+      bp += al(sizeof(PNode) * std::max<long long>(1, f->n_nodes));
       if (nprob == 1) {
         DML_CK(cudaMemcpyAsync(f->nodes, node_log.p, sizeof(ClassifyNode) * f->n_nodes,
                                cudaMemcpyDeviceToDevice, s));
@@ -824,14 +845,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     DML_CK(cudaStreamSynchronize(s));
     finish_stats(st);
   } catch (...) {
-    for (dml_forest* f : forests) {
-      if (f) {
-        cudaFree(f->nodes);
-        cudaFree(f->probs);
-        cudaFree(f->pnodes);
-        delete f;
-      }
-    }
+    for (dml_forest* f : forests) dml_forest_free(f);
     release_all();
     cudaStreamSynchronize(s);
     throw;
@@ -840,11 +854,14 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
 }
 
 dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s) {
-  cudaFree(f->pnodes);
-  f->pnodes = nullptr;
-  if (cudaMalloc(&f->pnodes, sizeof(PNode) * std::max<long long>(1, f->n_nodes)) != cudaSuccess) {
-    set_error("device allocation failed for the predict layout");
-    return DML_ERR_OOM;
+  if (!f->block) {  // forests of a fit have theirs in the fit's block
+    cudaFree(f->pnodes);
+    f->pnodes = nullptr;
+    if (cudaMalloc(&f->pnodes, sizeof(PNode) * std::max<long long>(1, f->n_nodes)) !=
+        cudaSuccess) {
+      set_error("device allocation failed for the predict layout");
+      return DML_ERR_OOM;
+    }
   }
   int g = (int)std::min<long long>(8192, (f->n_nodes + 255) / 256 + 1);
   k_to_pnodes<<<g, 256, 0, s>>>(f->nodes, f->n_nodes, f->probs, f->n_classes, f->task, f->pnodes);

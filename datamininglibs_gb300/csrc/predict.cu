@@ -537,9 +537,16 @@ dml_status dml_set_device(int32_t device) {
 
 void dml_forest_free(dml_forest* f) {
   if (!f) return;
-  cudaFree(f->nodes);
-  cudaFree(f->probs);
-  cudaFree(f->pnodes);
+  if (f->block) {
+    if (f->block->refs.fetch_sub(1) == 1) {
+      cudaFree(f->block->base);
+      delete f->block;
+    }
+  } else {
+    cudaFree(f->nodes);
+    cudaFree(f->probs);
+    cudaFree(f->pnodes);
+  }
   delete f;
 }
 
