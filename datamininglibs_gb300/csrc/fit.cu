@@ -342,6 +342,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     unsigned* d_max = (unsigned*)alloc(sizeof(unsigned) * nprob);
     DML_CK(cudaMemsetAsync(d_err, 0, sizeof(int) * 4, s));
     DML_CK(cudaMemsetAsync(d_max, 0, sizeof(unsigned) * nprob, s));
+    std::vector<PrepJob> jobs(nprob);
+    long long sum_nx = 0;
     for (int i = 0; i < nprob; ++i) {
       const dml_fit_desc& d = descs[i];
       ProbDesc& P = hp[i];
@@ -357,17 +359,27 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
         H.y = dy;
       }
       P.X = H.X;
-      long long nx = P.N * P.F;
-      int grid = (int)std::min<long long>(4096, (nx + 255) / 256);
-      k_validate<<<grid, 256, 0, s>>>(H.X, nx, H.y, P.N, P.task, P.C, d_err, d_max + i);
-      DML_CK(cudaGetLastError());
-      ++st.launches;
       if (P.task == 0)
         H.lab = (int*)alloc(sizeof(int) * P.N);
       else
         H.q = (long long*)alloc(sizeof(long long) * P.N);
       P.lab = H.lab;
       P.q = H.q;
+      jobs[i] = PrepJob{H.X, P.N * P.F, H.y, P.N, P.task, P.C, 0, H.lab, H.q};
+      sum_nx += P.N * P.F;
+    }
+    // one launch validates every problem (about 64 values a thread overall),
+    // one prepares the targets once the regression scales are known
+    const unsigned prep_x = (unsigned)std::max<long long>(
+        16, std::min<long long>(4096, sum_nx / (256 * 64) / nprob));
+    PrepJob* d_jobs = (PrepJob*)alloc(sizeof(PrepJob) * nprob);
+    DML_CK(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(PrepJob) * nprob, cudaMemcpyHostToDevice,
+                           s));
+    for (int j0 = 0; j0 < nprob; j0 += 65535) {  // grid.y holds at most 65535 problems
+      const int nj = std::min(65535, nprob - j0);
+      k_validate_all<<<dim3(prep_x, (unsigned)nj), 256, 0, s>>>(d_jobs + j0, d_err, d_max + j0);
+      DML_CK(cudaGetLastError());
+      ++st.launches;
     }
     int h_err[4] = {0, 0, 0, 0};
     std::vector<unsigned> h_max(nprob);
@@ -388,14 +400,21 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       throw InvalidArg{};
     }
     for (int i = 0; i < nprob; ++i) {
-      ProbDesc& P = hp[i];
       float mx;
       std::memcpy(&mx, &h_max[i], 4);
-      P.S = P.task == 1 ? quant_scale_from_max(mx, P.N) : 0;
-      int grid = (int)std::min<long long>(4096, (P.N + 255) / 256);
-      k_prep_targets<<<grid, 256, 0, s>>>(ph[i].y, P.N, P.task, P.S, ph[i].lab, ph[i].q);
+      hp[i].S = hp[i].task == 1 ? quant_scale_from_max(mx, hp[i].N) : 0;
+      jobs[i].S = hp[i].S;
+    }
+    DML_CK(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(PrepJob) * nprob, cudaMemcpyHostToDevice,
+                           s));
+    for (int j0 = 0; j0 < nprob; j0 += 65535) {
+      k_prep_all<<<dim3(prep_x, (unsigned)std::min(65535, nprob - j0)), 256, 0, s>>>(d_jobs + j0);
       DML_CK(cudaGetLastError());
       ++st.launches;
+    }
+    for (int i = 0; i < nprob; ++i) {
+      ProbDesc& P = hp[i];
+      const int grid = (int)std::min<long long>(4096, (P.N + 255) / 256);
       if (descs[i].balanced) {  // per-class row lists for the balanced bootstrap
         long long* off = (long long*)alloc(sizeof(long long) * (P.C + 1));
         int* rows = (int*)alloc(sizeof(int) * P.N);

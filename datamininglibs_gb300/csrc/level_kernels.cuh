@@ -642,8 +642,8 @@ __global__ void __launch_bounds__(256) k_emit(EmitArgs a) {
 // Checks the frame (finite features, integral labels in [0, C)) and gathers
 // max |y| for the regression fixed-point scale.  err bits: 1 = non-finite
 // feature, 2 = bad label, 4 = non-finite target.
-__global__ void k_validate(const float* X, long long nX, const float* y, long long N, int task,
-                           int C, int* err, unsigned* maxabs) {
+__device__ void validate_range(const float* X, long long nX, const float* y, long long N,
+                               int task, int C, int* err, unsigned* maxabs) {
   long long stride = (long long)gridDim.x * blockDim.x;
   int e = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nX; i += stride) {
@@ -663,9 +663,12 @@ __global__ void k_validate(const float* X, long long nX, const float* y, long lo
   if (e) atomicOr(err, e);
   if (task == 1) atomicMax(maxabs, mx);
 }
+__global__ void k_validate(const float* X, long long nX, const float* y, long long N, int task,
+                           int C, int* err, unsigned* maxabs) {
+  validate_range(X, nX, y, N, task, C, err, maxabs);
+}
 
-__global__ void k_prep_targets(const float* y, long long N, int task, int S, int* lab,
-                               long long* q) {
+__device__ void prep_range(const float* y, long long N, int task, int S, int* lab, long long* q) {
   long long stride = (long long)gridDim.x * blockDim.x;
   const double sc = pow2d(S);
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
@@ -674,6 +677,29 @@ __global__ void k_prep_targets(const float* y, long long N, int task, int S, int
     else
       q[i] = __double2ll_rn((double)y[i] * sc);
   }
+}
+__global__ void k_prep_targets(const float* y, long long N, int task, int S, int* lab,
+                               long long* q) {
+  prep_range(y, N, task, S, lab, q);
+}
+
+// The same for every problem of a fit in one launch each: problem blockIdx.y.
+struct PrepJob {
+  const float* X;
+  long long nX;
+  const float* y;
+  long long N;
+  int task, C, S;
+  int* lab;
+  long long* q;
+};
+__global__ void k_validate_all(const PrepJob* jobs, int* err, unsigned* maxabs) {
+  const PrepJob j = jobs[blockIdx.y];
+  validate_range(j.X, j.nX, j.y, j.N, j.task, j.C, err, maxabs + blockIdx.y);
+}
+__global__ void k_prep_all(const PrepJob* jobs) {
+  const PrepJob j = jobs[blockIdx.y];
+  prep_range(j.y, j.N, j.task, j.S, j.lab, j.q);
 }
 
 // One launch for every (level, forest) segment of a batch: nodes from the
