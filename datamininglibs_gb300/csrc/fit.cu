@@ -24,7 +24,7 @@ static_assert(dml::kNumQ == DML_NUM_QUEUES && dml::kQWarp == DML_Q_WARP32 &&
                   dml::kQRfBig == DML_Q_RF_BIG && dml::kQRfW2 == DML_Q_RF_W64 &&
                   dml::kQRfW4 == DML_Q_RF_W128 && dml::kQRfW8 == DML_Q_RF_W256 &&
                   dml::kQG16 == DML_Q_GROUP16 && dml::kQG8 == DML_Q_GROUP8 &&
-                  dml::kQRfW16 == DML_Q_RF_W512,
+                  dml::kQRfW16 == DML_Q_RF_W512 && dml::kQErtW == DML_Q_ERT_W256,
               "node classes of the engine and of include/dml.h agree");
 
 namespace dml {
@@ -712,13 +712,13 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       search_ms_total += sm;
       if (trace)
         fprintf(stderr,
-                "[dml] level %2d nodes %9d | g8 %8d %7.2f | g16 %8d %7.2f | w32 %8d %7.2f | ert %6d "
-                "%7.2f | w64 %7d %7.2f | w128 %7d %7.2f | w256 %7d %7.2f | w512 %7d %7.2f | cta %7d "
-                "%7.2f | big %5d %7.2f | search %8.2f ms\n",
+                "[dml] level %2d nodes %9d | g8 %8d %7.2f | g16 %8d %7.2f | w32 %8d %7.2f | "
+                "ertw %7d %7.2f | ert %6d %7.2f | w64 %7d %7.2f | w128 %7d %7.2f | w256 %7d %7.2f | "
+                "w512 %7d %7.2f | cta %7d %7.2f | big %5d %7.2f | search %8.2f ms\n",
                 depth, n, qc[kQG8], qms[kQG8], qc[kQG16], qms[kQG16], qc[kQWarp], qms[kQWarp],
-                qc[kQErt], qms[kQErt], qc[kQRfW2], qms[kQRfW2], qc[kQRfW4], qms[kQRfW4], qc[kQRfW8],
-                qms[kQRfW8], qc[kQRfW16], qms[kQRfW16], qc[kQRfSmall], qms[kQRfSmall], qc[kQRfBig],
-                qms[kQRfBig], sm);
+                qc[kQErtW], qms[kQErtW], qc[kQErt], qms[kQErt], qc[kQRfW2], qms[kQRfW2], qc[kQRfW4],
+                qms[kQRfW4], qc[kQRfW8], qms[kQRfW8], qc[kQRfW16], qms[kQRfW16], qc[kQRfSmall],
+                qms[kQRfSmall], qc[kQRfBig], qms[kQRfBig], sm);
       if (trace) {  // per class: entries and tries x entries searched at this level
         static long long prev[kStatWords];
         long long cur_st[kStatWords];

@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
 // memory sort), RF big (CTA, global sort).  Queue order does not affect
 // results, only scheduling.
 enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kQRfW2 = 4, kQRfW4 = 5, kQRfW8 = 6,
-       kQG16 = 7, kQG8 = 8, kQRfW16 = 9, kNumQ = 10 };
+       kQG16 = 7, kQG8 = 8, kQRfW16 = 9, kQErtW = 10, kNumQ = 11 };
 
 struct Queues {
   int* list[kNumQ];
@@ -333,7 +333,7 @@ __device__ __forceinline__ int queue_of(const ProbDesc& P, int ecnt, const Queue
   if (ecnt <= 8) return kQG8;
   if (ecnt <= 16) return kQG16;
   if (ecnt <= 32) return kQWarp;
-  if (P.algo == 1) return kQErt;
+  if (P.algo == 1) return ecnt <= 256 ? kQErtW : kQErt;
   if (ecnt <= 64 && Q.rf_warp_max >= 64) return kQRfW2;
   if (ecnt <= 128 && Q.rf_warp_max >= 128) return kQRfW4;
   if (ecnt <= 256 && Q.rf_warp_max >= 256) return kQRfW8;

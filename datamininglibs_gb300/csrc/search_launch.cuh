@@ -6,6 +6,7 @@
 #include "engine.h"
 #include "level_kernels.cuh"
 #include "big_rf.cuh"
+#include "ert_warp.cuh"
 
 namespace dml {
 
@@ -48,6 +49,8 @@ void launch_search_cw(int q, const LevelArgs& a, int count, cudaStream_t s) {
   } else if (q == kQRfW16) {
     constexpr int wpb = warp_rf_wpb<16>();
     k_warp_rf<16, CW><<<std::max(1, std::min((count + wpb - 1) / wpb, 1 << 20)), 32 * wpb, 0, s>>>(b);
+  } else if (q == kQErtW) {
+    k_ert_warp<8><<<wblocks, 256, 0, s>>>(b);
   } else if (q == kQErt) {
     k_ert_cta<kBlock><<<std::min(count, 1 << 20), kBlock, 0, s>>>(b);
   } else {

@@ -63,11 +63,11 @@ class ForestInfo(ctypes.Structure):
                 ("fit_ms", ctypes.c_double)]
 
 
-NUM_QUEUES = 10
+NUM_QUEUES = 11
 # kernel that searches each node class (DML_Q_* in include/dml.h)
 QUEUE_KERNELS = ["k_group_nodes<32>", "k_ert_cta", "k_rf_smem", "k_rf_big_items+k_rf_big_decide",
                  "k_warp_rf<2>", "k_warp_rf<4>", "k_warp_rf<8>", "k_group_nodes<16>",
-                 "k_group_nodes<8>", "k_warp_rf<16>"]
+                 "k_group_nodes<8>", "k_warp_rf<16>", "k_ert_warp<8>"]
 
 
 class FitStats(ctypes.Structure):

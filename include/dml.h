@@ -99,7 +99,7 @@ typedef struct {
  * and the kernels that search them. */
 enum {
   DML_Q_WARP32 = 0,   /* <= 32 entries, one warp per node (k_group_nodes<32>) */
-  DML_Q_ERT = 1,      /* ERT, > 32 entries, one CTA per node (k_ert_cta) */
+  DML_Q_ERT = 1,      /* ERT, > 256 entries, one CTA per node (k_ert_cta) */
   DML_Q_RF_SMEM = 2,  /* RF, above the warp classes up to the tuned cap (at most 4096
                        * entries), CTA, shared-memory sort (k_rf_smem) */
   DML_Q_RF_BIG = 3,   /* RF, > 4096 entries, per-try items (k_rf_big_items + _decide) */
@@ -109,7 +109,8 @@ enum {
   DML_Q_GROUP16 = 7,  /* <= 16 entries, 16 lanes per node (k_group_nodes<16>) */
   DML_Q_GROUP8 = 8,   /* <= 8 entries, 8 lanes per node (k_group_nodes<8>) */
   DML_Q_RF_W512 = 9,  /* RF, 257..512 entries (k_warp_rf<16>) */
-  DML_NUM_QUEUES = 10
+  DML_Q_ERT_W256 = 10, /* ERT, 33..256 entries, one warp per node (k_ert_warp<8>) */
+  DML_NUM_QUEUES = 11
 };
 
 /* Fit statistics of the last dml_fit/dml_fit_batched on this thread. */
