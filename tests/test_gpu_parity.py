@@ -104,6 +104,30 @@ def test_batched_uneven_forests_match_single_fits(dml):
         _assert_same_model(m, nodes, pr)
 
 
+def test_forests_of_one_fit_free_independently(dml):
+    """The forests of one fit share one device allocation: each stays whole
+    (export and predict equal the oracle's) while the others are freed in any
+    order, and freeing the last releases the block."""
+    probs = synth.uneven_problems(5, seed=9, n_range=(300, 2000), f_range=(6, 20))
+    specs = [dict(X=X, y=y, algo=i % 2, n_trees=3, K=0, max_depth=8, min_node_size=5,
+                  n_classes=c, seed=40 + i) for i, (X, y, c) in enumerate(probs)]
+    batch = dml.fit_batched(specs)
+    models = []
+    for sp in specs:
+        sp = dict(sp)
+        X, y = sp.pop("X"), sp.pop("y")
+        models.append((oracle.fit(X, y, **sp), X))
+    for i in (3, 0, 4, 1, 2):
+        batch[i].free()
+        for j in range(len(specs)):
+            if j in (3, 0, 4, 1, 2)[: (3, 0, 4, 1, 2).index(i) + 1]:
+                continue
+            m, X = models[j]
+            nodes, pr = batch[j].export()
+            _assert_same_model(m, nodes, pr, tag="forest %d after freeing %d" % (j, i))
+            assert np.array_equal(batch[j].predict(X), oracle.predict(m, X)), (j, i)
+
+
 def test_repeated_fits_bitwise_identical(dml):
     X, y = synth.ert_binary(2500, 20, seed=41)
     kw = dict(algo=0, n_trees=8, K=5, max_depth=12, min_node_size=5, n_classes=2, seed=4)
