@@ -433,8 +433,13 @@ void worker_main(dml_server* s, bool small) {
     if (s->stop && q.empty() && !any_busy) break;
     if (!progressed) {
       if (any_busy) {
+        // the small lane polls its batches without sleeping (a sleep rounds up
+        // to tens of microseconds); the large lane naps between polls
         lk.unlock();
-        std::this_thread::sleep_for(std::chrono::microseconds(10));
+        if (small)
+          std::this_thread::yield();
+        else
+          std::this_thread::sleep_for(std::chrono::microseconds(10));
       } else {
         cv.wait_for(lk, std::chrono::milliseconds(5), [&] { return s->stop || !q.empty(); });
       }
