@@ -80,13 +80,16 @@ __global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict_
 // order, as k_predict does.
 constexpr int kPSplit = 8;
 constexpr int kPRows = kPredBlock / kPSplit;  // 16
+// a feature's 16 rows, padded to 17 floats: lanes reading different features
+// of one row meet different banks
+constexpr int kPStride = kPRows + 1;
 
 template <int TASK>
 __global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __restrict__ nodes,
                                                               int n_trees, int C, int F,
                                                               const float* __restrict__ X,
                                                               long long N, float* __restrict__ out) {
-  extern __shared__ float psm[];  // xs [F][kPRows], then votes [kPRows][C] or values [kPRows][n_trees]
+  extern __shared__ float psm[];  // xs [F][kPStride], then votes [kPRows][C] or values [kPRows][n_trees]
   const long long row0 = (long long)blockIdx.x * kPRows;
   const int rows = N - row0 < kPRows ? (int)(N - row0) : kPRows;
   const int g = threadIdx.x % kPSplit;
@@ -94,10 +97,10 @@ __global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __res
   float* xs = psm;
   for (int e = threadIdx.x; e < F * kPRows; e += kPredBlock) {
     const int f = e / kPRows, rr = e % kPRows;
-    xs[e] = rr < rows ? __ldg(X + (long long)f * N + row0 + rr) : 0.0f;
+    xs[f * kPStride + rr] = rr < rows ? __ldg(X + (long long)f * N + row0 + rr) : 0.0f;
   }
-  int* votes = reinterpret_cast<int*>(psm + F * kPRows);
-  float* vals = psm + F * kPRows + r * n_trees;
+  int* votes = reinterpret_cast<int*>(psm + F * kPStride);
+  float* vals = psm + F * kPStride + r * n_trees;
   if (TASK == 0)
     for (int i = threadIdx.x; i < kPRows * C; i += kPredBlock) votes[i] = 0;
   __syncthreads();
@@ -117,7 +120,7 @@ __global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __res
 #pragma unroll
         for (int j = 0; j < 4; ++j)
           if (lf[j].x >= 0) {
-            lf[j] = __ldg(nd + (goes_left(xs[lf[j].y * kPRows + r], __int_as_float(lf[j].z))
+            lf[j] = __ldg(nd + (goes_left(xs[lf[j].y * kPStride + r], __int_as_float(lf[j].z))
                                     ? lf[j].x
                                     : lf[j].x + 1));
             more = more || lf[j].x >= 0;
@@ -175,8 +178,8 @@ dml_status predict_device(const dml_forest* f, const float* dX, long long n_rows
   if (n_rows <= 0) return DML_OK;
   // staged rows when the tile (features, votes or per-tree values) fits 48 KB
   const size_t split_sm =
-      sizeof(float) * kPRows *
-      ((size_t)f->n_features + (f->task == DML_CLASSIFICATION ? f->n_classes : f->n_trees));
+      sizeof(float) * ((size_t)kPStride * f->n_features +
+                       (size_t)kPRows * (f->task == DML_CLASSIFICATION ? f->n_classes : f->n_trees));
   if (split_sm <= 48 * 1024) {
     const long long tiles = (n_rows + kPRows - 1) / kPRows;
     if (f->task == DML_CLASSIFICATION)

@@ -44,9 +44,12 @@ namespace {
 constexpr int kTileRows = 128;      // large lane: rows per tile (one thread per row)
 constexpr int kSplit = 8;           // small lane: threads per row
 constexpr int kSplitRows = kTileRows / kSplit;
+// a feature's 16 rows padded to 17 words in shared memory: lanes reading
+// different features of one row meet different banks
+constexpr int kSplitStride = kSplitRows + 1;
 constexpr int kSplitMaxTrees = 512;  // small-lane regression keeps [rows][trees] leaf values
 constexpr int kSplitMaxFeatures = 1024;  // small-lane tiles stage [features][16 rows] in shared memory
-constexpr int kSplitSmem = 96 * 1024;
+constexpr int kSplitSmem = 112 * 1024;  // >= 4 * (17 * 1024 features + 16 * 512 trees)
 
 struct PredTile {
   const PNode* nodes;
@@ -105,17 +108,17 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles(const PredTile* __r
 // order by one thread.
 __global__ void __launch_bounds__(kTileRows) k_predict_tiles_split(
     const PredTile* __restrict__ tiles) {
-  extern __shared__ int sm[];  // xs [F][kSplitRows], then votes [kSplitRows][C] or values
+  extern __shared__ int sm[];  // xs [F][kSplitStride], then votes [kSplitRows][C] or values
   const PredTile t = tiles[blockIdx.x];
   const int g = threadIdx.x % kSplit;
   const int r = threadIdx.x / kSplit;
   const bool act = r < t.rows;
   const long long row = (long long)t.row0 + r;
   float* xs = reinterpret_cast<float*>(sm);
-  int* acc = sm + t.F * kSplitRows;
+  int* acc = sm + t.F * kSplitStride;
   for (int e = threadIdx.x; e < t.F * kSplitRows; e += kTileRows) {
     const int f = e / kSplitRows, rr = e % kSplitRows;
-    xs[e] = rr < t.rows ? t.X[(long long)f * t.n + t.row0 + rr] : 0.0f;
+    xs[f * kSplitStride + rr] = rr < t.rows ? t.X[(long long)f * t.n + t.row0 + rr] : 0.0f;
   }
   if (t.task == 0)
     for (int i = threadIdx.x; i < kSplitRows * t.C; i += kTileRows) acc[i] = 0;
@@ -125,7 +128,7 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles_split(
     for (int k = g; k < t.n_trees; k += kSplit) {
       int4 p = __ldg(reinterpret_cast<const int4*>(t.nodes) + k);
       while (p.x >= 0) {
-        const float x = xs[p.y * kSplitRows + r];
+        const float x = xs[p.y * kSplitStride + r];
         const int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
         p = __ldg(reinterpret_cast<const int4*>(t.nodes) + nx);
       }
@@ -364,7 +367,7 @@ bool launch_batch(dml_server* s, Slot& sl) {
       }
       if (pass == 0)
         shm_split = std::max(
-            shm_split, (int)sizeof(int) * (kSplitRows * f->n_features +
+            shm_split, (int)sizeof(int) * (kSplitStride * f->n_features +
                                            (f->task == DML_CLASSIFICATION ? kSplitRows * r.width
                                                                           : kSplitRows * f->n_trees)));
       else
@@ -402,6 +405,8 @@ void worker_main(dml_server* s, bool small) {
   cudaSetDevice(s->device);
   auto& q = small ? s->q_small : s->q_large;
   auto& cv = s->cv_work[small ? 1 : 0];
+  const auto pace = std::chrono::microseconds(s->cfg.max_wait_us);
+  Clock::time_point last_launch = Clock::now() - std::chrono::seconds(1);
   while (true) {
     bool progressed = reap(s, small);
     bool idle = true;
@@ -410,11 +415,18 @@ void worker_main(dml_server* s, bool small) {
     for (Slot& sl : s->slots) {
       if (sl.small != small || sl.batch.busy) continue;
       bool pending;
+      long long waiting = 0;
       {
         std::lock_guard<std::mutex> lk(s->mu);
         pending = !q.empty();
+        if (small)
+          for (auto& r : q) waiting += r->n - r->next_row;
       }
       if (!pending) continue;
+      // with batches in flight, the small lane launches the next one after
+      // max_wait_us (or a batch's worth of rows), so that requests arriving
+      // meanwhile share it
+      if (small && !idle && Clock::now() - last_launch < pace && waiting < s->small_rows) continue;
       if (small && idle && s->cfg.max_wait_us > 0) {
         // an idle lane lets a batch fill briefly while few rows wait
         std::unique_lock<std::mutex> lk(s->mu);
@@ -424,7 +436,11 @@ void worker_main(dml_server* s, bool small) {
           cv.wait_for(lk, std::chrono::microseconds(s->cfg.max_wait_us));
         idle = false;
       }
-      progressed |= launch_batch(s, sl);
+      if (launch_batch(s, sl)) {
+        progressed = true;
+        idle = false;
+        if (small) last_launch = Clock::now();
+      }
     }
     bool any_busy = false;
     for (Slot& sl : s->slots)
