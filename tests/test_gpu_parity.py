@@ -191,7 +191,7 @@ def test_big_nodes_with_signed_zeros_and_missing(dml):
         _assert_same_model(m, nodes, probs, task)
 
 
-@pytest.mark.parametrize("n_rows", [1, 2, 3, 33, 65, 129, 257, 513, 4097])
+@pytest.mark.parametrize("n_rows", [1, 2, 3, 33, 65, 129, 257, 513, 1025, 2049, 4097])
 def test_tiny_and_boundary_sizes(dml, n_rows):
     X, y = synth.rf_multiclass(n_rows, 5, n_classes=2, n_int=1, seed=n_rows)
     for algo in (0, 1):
