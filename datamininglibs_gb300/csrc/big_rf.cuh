@@ -1,13 +1,16 @@
 // RF split search for large nodes (more entries than fit a shared-memory
 // sort): one CTA per (node, try) work item on a persistent grid, each with its
-// own global scratch.  The sort is an LSD radix sort (8-bit digits) over tiles
-// of 2048 pairs: each warp loads its 256-pair chunk with eight loads in flight,
-// ranks digits stably within warps (digit_peers), and the tile is reordered in
-// shared memory so that every digit's run is written to global memory as one
-// contiguous stretch.  The boundary scan gives each thread 8 consecutive
-// sorted elements (one block scan of packed class counts per 2048 elements).
-// A second kernel applies the try loop (gpurf.cu:177-245) per node and
-// partitions its entries.
+// own global scratch.  The item gathers its keys (value ranks) and the node's
+// packed (label, weight) values, counting the digit histograms of the keys'
+// significant bytes on the way.  The sort is an LSD radix sort (8-bit digits)
+// over tiles of 2048 pairs: each warp loads its 256-pair chunk with eight loads
+// in flight, ranks digits stably within warps (digit_peers), and the tile is
+// reordered in shared memory so that every digit's run is written to global
+// memory as one contiguous stretch.  The boundary scan gives each thread 8
+// consecutive sorted elements (one block scan of packed class counts per 2048
+// elements) and keeps the entropy incrementally.  A second kernel applies the
+// try loop (gpurf.cu:177-245) per node and partitions its entries.  The
+// shared-memory kernel for mid-size nodes (k_rf_smem) is at the end.
 #pragma once
 #include "fit_kernels.cuh"
 #include "warp_rf.cuh"

@@ -8,8 +8,9 @@ namespace dml {
 
 // ============================================================== tiny nodes
 // Groups of G lanes (G = 8, 16 or 32) per node with at most G entries, 32/G
-// nodes per warp: entries live in lanes.  RF sorts the (key, lane) pairs with a
-// register bitonic network; prefix class counts come from group scans.  Same
+// nodes per warp: entries live in lanes.  RF sorts rank << 5 | lane keys with a
+// register bitonic network, and the entropy numerator of every boundary comes
+// from one group scan of each entry's own-class change.  Same
 // candidate rules as the CTA kernels.  Every shuffle and ballot names only the
 // group's lanes, so groups of one warp may hold nodes of different forests
 // (RF and ERT, classification and regression) and run different try counts.
@@ -299,9 +300,10 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
 }
 
 // ============================================================ work queues
-// Node classes: tiny (<= 32 entries, warp), ERT (CTA), RF small (CTA, shared
-// memory sort), RF big (CTA, global sort).  Queue order does not affect
-// results, only scheduling.
+// Node classes: tiny (<= 8, 16, 32 entries: lane groups), RF warp (up to 64,
+// 128, 256, 512 entries), ERT warp (up to 256), ERT (CTA), RF small (CTA,
+// shared-memory sort), RF big (per-try items, global sort).  Queue order does
+// not affect results, only scheduling.
 enum { kQWarp = 0, kQErt = 1, kQRfSmall = 2, kQRfBig = 3, kQRfW2 = 4, kQRfW4 = 5, kQRfW8 = 6,
        kQG16 = 7, kQG8 = 8, kQRfW16 = 9, kQErtW = 10, kNumQ = 11 };
 
