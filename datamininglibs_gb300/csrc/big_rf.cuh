@@ -203,12 +203,12 @@ struct BigArgs {
   int* nretry_out;
   int* big_index;          // node id -> index in `big` (for phase 2)
   uint32_t* pv;            // classification: label << 27 | weight per entry slot of the big nodes
-  long long* pq;           // regression: fixed-point target per entry slot of the big nodes
+  long long* pq;           // regression: packed (target, weight) per entry slot of the big nodes
 };
 
 // Per-entry values of the big nodes, once per level instead of a gather by
-// row per try: packed (label << 27 | weight) for classification, the target
-// for regression.
+// row per try: packed (label << 27 | weight) for classification, the packed
+// (target, weight) word (qw_pack) for regression.
 template <int CW>
 __global__ void __launch_bounds__(kBigBlock) k_big_pack(BigArgs b) {
   const LevelArgs& a = b.L;
@@ -222,40 +222,37 @@ __global__ void __launch_bounds__(kBigBlock) k_big_pack(BigArgs b) {
                   (uint32_t)(a.wA ? __ldg(a.wA + e) : 1);
       }
     } else if (P.task != 0 && b.pq) {
+      const int wb = qw_bits(P.N);
       for (int i = threadIdx.x; i < nd.ecnt; i += kBigBlock) {
         const long long e = nd.ebeg + i;
-        b.pq[e] = __ldg(P.q + __ldg(a.rowsA + e));
+        b.pq[e] = qw_pack(__ldg(P.q + __ldg(a.rowsA + e)), a.wA ? __ldg(a.wA + e) : 1, wb);
       }
     }
   }
 }
 
-// Boundary scan of a sorted item: each thread owns `per` (1..8) consecutive
-// elements of every tile of 256 * per.  Classification items carry
-// (label << 27 | weight) through the sort (packed == true); regression items
-// carry the entry index into ew / eq.
-// INCR (classification): each thread keeps its values in registers and Q
-// incrementally along its elements (6 table terms an entry instead of 2C + 2
-// a boundary); worth it for 8 elements per thread.
+// Boundary scan of a sorted classification item, whose values are the packed
+// (label << 27 | weight) words: each thread owns `per` (1..8) consecutive
+// elements of every tile of 256 * per.  INCR: each thread keeps its values in
+// registers and Q incrementally along its elements (6 table terms an entry
+// instead of 2C + 2 a boundary); worth it for 8 elements per thread.
 template <int CW, bool INCR>
-__device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed, const int* ew,
-                             const long long* eq, int m, int per, const LNode& nd,
-                             const ProbDesc& P, const int* ncnt, const long long* H, long long prior,
-                             unsigned long long* scan64, float* out_g, int* out_p, long long* out_nl,
-                             long long* out_sl, unsigned long long (&outL)[CW]) {
+__device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, int m, int per,
+                             const LNode& nd, const ProbDesc& P, const int* ncnt,
+                             const long long* H, long long prior, unsigned long long* scan64,
+                             float* out_g, int* out_p, long long* out_nl,
+                             unsigned long long (&outL)[CW]) {
   const int C = P.C;
   const int ml = max(1, P.min_leaf);
   int Nt[2 * CW];
 #pragma unroll
-  for (int c = 0; c < 2 * CW; ++c) Nt[c] = (packed && c < C) ? ncnt[c] : 0;
-  float bg = -FLT_MAX;  // regression
-  int bp = -1;
-  NumBest nb;  // classification
+  for (int c = 0; c < 2 * CW; ++c) Nt[c] = c < C ? ncnt[c] : 0;
+  NumBest nb;
   nb.init();
-  long long bnl = 0, bsl = 0;
+  long long bnl = 0;
   unsigned long long bL[CW];
   unsigned long long carry[CW];
-  long long carry_n = 0, carry_s = 0;
+  long long carry_n = 0;
 #pragma unroll
   for (int j = 0; j < CW; ++j) {
     bL[j] = 0;
@@ -264,19 +261,15 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
   for (int base = 0; base < m; base += kBigBlock * per) {
     const int p0 = base + threadIdx.x * per;
     const uint32_t prevk0 = p0 > 0 && p0 - 1 < m ? sk[p0 - 1] : 0u;
-    // per-thread totals (classification: from the packed values, which the
-    // scan below reads again, and a bit mask of the key boundaries;
-    // regression: keys, weights and targets kept in registers)
-    long long tn = 0, ts = 0;
+    // per-thread totals from the packed values (which the scan below reads
+    // again) and a bit mask of the key boundaries
+    long long tn = 0;
     unsigned long long tl[CW];
 #pragma unroll
     for (int c = 0; c < CW; ++c) tl[c] = 0;
-    uint32_t kk[kBigPer];
-    int w[kBigPer];
-    long long q[kBigPer];
     uint32_t vq[kBigPer];  // INCR: the packed values, consumed from vq[0]
-    unsigned bnd = 0;  // classification: bit j set when element j starts a new key
-    if (packed) {
+    unsigned bnd = 0;  // bit j set when element j starts a new key
+    {
       uint32_t prev = prevk0;
 #pragma unroll
       for (int j = 0; j < kBigPer; ++j) {
@@ -297,49 +290,23 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
                      (lj == 2 * c + 1 ? ((unsigned long long)wj << 32) : 0ull);
         }
       }
-    } else {
-#pragma unroll
-      for (int j = 0; j < kBigPer; ++j) {
-        const int p = p0 + j;
-        if (j < per && p < m) {
-          kk[j] = sk[p];
-          const int e = (int)sv[p];
-          w[j] = ew ? ew[e] : 1;
-          q[j] = eq[e];
-        } else {
-          kk[j] = 0xFFFFFFFFu;
-          w[j] = 0;
-          q[j] = 0;
-        }
-        tn += w[j];
-        ts += q[j] * (long long)w[j];
-      }
     }
-    // one block scan of the row count and the packed class counts (or the
-    // regression sum) of every thread's elements
+    // one block scan of the row count and the packed class counts of every
+    // thread's elements
     unsigned long long sv_[CW + 1], tot[CW + 1];
     sv_[0] = (unsigned long long)tn;
 #pragma unroll
-    for (int c = 0; c < CW; ++c) sv_[1 + c] = packed ? tl[c] : (c == 0 ? (unsigned long long)ts : 0ull);
+    for (int c = 0; c < CW; ++c) sv_[1 + c] = tl[c];
     block_excl_scan_n<kBigBlock, CW + 1>(sv_, tot, scan64);
     long long run_n = carry_n + (long long)sv_[0];
     carry_n += (long long)tot[0];
-    long long run_s = 0;
     unsigned long long runL[CW];
-    if (packed) {
 #pragma unroll
-      for (int c = 0; c < CW; ++c) {
-        runL[c] = carry[c] + sv_[1 + c];
-        carry[c] += tot[1 + c];
-      }
-    } else {
-      run_s = carry_s + (long long)sv_[1];
-      carry_s += (long long)tot[1];
-#pragma unroll
-      for (int c = 0; c < CW; ++c) runL[c] = 0;
+    for (int c = 0; c < CW; ++c) {
+      runL[c] = carry[c] + sv_[1 + c];
+      carry[c] += tot[1 + c];
     }
-    uint32_t prevk = prevk0;
-    if (packed && INCR) {
+    if (INCR) {
       // Q computed in full at the first boundary that meets min_leaf, then
       // moved entry by entry while boundaries remain (h(nL), h(nR) carried)
       long long Q = 0, hl = 0, hr = 0;
@@ -386,8 +353,8 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
           runL[c] += (labj == 2 * c ? (unsigned long long)wj : 0ull) |
                      (labj == 2 * c + 1 ? ((unsigned long long)wj << 32) : 0ull);
       }
-    } else if (packed) {
-      // classification: a rolled loop that re-reads each label|weight value
+    } else {
+      // a rolled loop that re-reads each label|weight value
       // (the class terms unrolled eight times overflow the instruction cache);
       // boundaries are compared on their exact gain numerators P - Q
 #pragma unroll 1
@@ -419,35 +386,106 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, bool packed
           runL[c] += (labj == 2 * c ? (unsigned long long)wj : 0ull) |
                      (labj == 2 * c + 1 ? ((unsigned long long)wj << 32) : 0ull);
       }
-    } else {
-      // regression: the gathered weights and targets stay in registers
-#pragma unroll
-      for (int j = 0; j < kBigPer; ++j) {
-        const int p = p0 + j;
-        if (j < per && p < m && p > 0 && prevk < kk[j]) {
-          const long long nr = (long long)nd.n - run_n;
-          if (run_n >= ml && nr >= ml) {
-            const float g = variance_gain(run_n, run_s, nr, nd.sum - run_s, P.S);
-            if (bp < 0 || g > bg) {
-              bg = g;
-              bp = p;
-              bnl = run_n;
-              bsl = run_s;
-            }
-          }
-        }
-        prevk = kk[j];
-        run_n += w[j];
-        run_s += q[j] * (long long)w[j];
-      }
     }
   }
-  *out_g = packed ? nb.gain(nd.n) : bg;
-  *out_p = packed ? nb.p : bp;
+  *out_g = nb.gain(nd.n);
+  *out_p = nb.p;
   *out_nl = bnl;
-  *out_sl = bsl;
 #pragma unroll
   for (int c = 0; c < CW; ++c) outL[c] = bL[c];
+}
+
+// Boundary scan of a sorted regression item, whose values index eq, the
+// entries' packed (target, weight) words; `per` (1..8) consecutive elements a
+// thread per tile as above.  Out of line, so that its registers do not weigh
+// on the classification scan of the same kernels.  The float-float gain is
+// evaluated only at boundaries whose upper bound (variance_gain_bounds)
+// reaches t, the larger of the best gain so far and the lower bounds of the
+// thread's boundaries in the tile: a boundary below t can neither be nor tie
+// the best.  n, sum: the node's weight and weighted target sum; S: the target
+// scale; N: the problem's rows (the packing).
+static __device__ __noinline__ void big_boundary_reg(const uint32_t* sk, const uint32_t* sv,
+                                                     const long long* eq, int m, int per,
+                                                     long long n, long long sum, int ml, int S,
+                                                     long long N, unsigned long long* scan64,
+                                                     float* out_g, int* out_p, long long* out_nl,
+                                                     long long* out_sl) {
+  const int wb = qw_bits(N);
+  const float rc = __frcp_rn(__ll2float_rn(n));
+  const float p2 = pow2f(-2 * S);
+  float bg = -FLT_MAX;
+  int bp = -1;
+  long long bnl = 0, bsl = 0;
+  long long carry_n = 0, carry_s = 0;
+  for (int base = 0; base < m; base += kBigBlock * per) {
+    const int p0 = base + threadIdx.x * per;
+    // weights and weighted targets in registers, a bit mask of the key
+    // boundaries
+    int w[kBigPer];
+    long long q[kBigPer];
+    unsigned bnd = 0;
+    long long tn = 0, ts = 0;
+    uint32_t prev = p0 > 0 && p0 - 1 < m ? sk[p0 - 1] : 0u;
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j) {
+      const int p = p0 + j;
+      w[j] = 0;
+      q[j] = 0;
+      if (j < per && p < m) {
+        const uint32_t kj = sk[p];
+        if (p > 0 && prev < kj) bnd |= 1u << j;
+        prev = kj;
+        const long long x = eq[sv[p]];
+        w[j] = qw_weight(x, wb);
+        q[j] = qw_target(x, wb) * w[j];
+      }
+      tn += w[j];
+      ts += q[j];
+    }
+    unsigned long long sv_[2] = {(unsigned long long)tn, (unsigned long long)ts}, tot[2];
+    block_excl_scan_n<kBigBlock, 2>(sv_, tot, scan64);
+    long long run_n = carry_n + (long long)sv_[0];
+    long long run_s = carry_s + (long long)sv_[1];
+    carry_n += (long long)tot[0];
+    carry_s += (long long)tot[1];
+    float hi[kBigPer];
+    unsigned cand = 0;
+    float t = bp < 0 ? -FLT_MAX : bg;
+    {
+      long long rn = run_n, rs = run_s;
+#pragma unroll
+      for (int j = 0; j < kBigPer; ++j) {
+        hi[j] = 0.0f;
+        const long long nr = n - rn;
+        if (((bnd >> j) & 1u) && rn >= ml && nr >= ml) {
+          float lo;
+          variance_gain_bounds((int)rn, rs, (int)nr, sum - rs, rc, p2, lo, hi[j]);
+          t = fmaxf(t, lo);
+          cand |= 1u << j;
+        }
+        rn += w[j];
+        rs += q[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kBigPer; ++j) {
+      if (((cand >> j) & 1u) && hi[j] >= t) {
+        const float g = variance_gain(run_n, run_s, n - run_n, sum - run_s, S);
+        if (bp < 0 || g > bg) {
+          bg = g;
+          bp = p0 + j;
+          bnl = run_n;
+          bsl = run_s;
+        }
+      }
+      run_n += w[j];
+      run_s += q[j];
+    }
+  }
+  *out_g = bg;
+  *out_p = bp;
+  *out_nl = bnl;
+  *out_sl = bsl;
 }
 
 template <int CW>
@@ -484,7 +522,6 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     // eight gathers in flight per thread; the keys' OR / AND and the digit
     // histograms of their significant bytes on the way
     const bool packed = P.task == 0;
-    const int* wts = a.wA ? a.wA + nd.ebeg : nullptr;
     const uint32_t* pv = b.pv ? b.pv + nd.ebeg : nullptr;
     const uint32_t* rk = P.rank ? P.rank + (long long)f * P.N : nullptr;
     const int nbytes = rk ? (32 - __clz(max(1ll, P.N - 1)) + 7) >> 3 : 4;
@@ -541,14 +578,19 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     const bool in2 = big_sort(k1, v1, k2, v2, m, diff, S);
     const uint32_t* sk = in2 ? k2 : k1;
     const uint32_t* sv = in2 ? v2 : v1;
-    // regression: the node's per-entry targets
-    const long long* eq = b.pq + nd.ebeg;
     float g;
     int p;
-    long long nl, sl;
+    long long nl, sl = 0;
     unsigned long long L[CW];
-    big_boundary<CW, true>(sk, sv, packed, wts, eq, m, kBigPer, nd, P, ncnt, a.H, s_prior, S.scan64, &g,
-                     &p, &nl, &sl, L);
+    if (packed) {
+      big_boundary<CW, true>(sk, sv, m, kBigPer, nd, P, ncnt, a.H, s_prior, S.scan64, &g, &p, &nl,
+                             L);
+    } else {
+      big_boundary_reg(sk, sv, b.pq + nd.ebeg, m, kBigPer, nd.n, nd.sum, max(1, P.min_leaf), P.S,
+                       P.N, S.scan64, &g, &p, &nl, &sl);
+#pragma unroll
+      for (int c = 0; c < CW; ++c) L[c] = 0;
+    }
     const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
     if (bp >= 0 && p == bp) {
       Cand c;
@@ -671,7 +713,7 @@ __global__ void __launch_bounds__(kBigBlock) k_rf_big_decide(BigArgs b) {
 // the boundaries with ceil(m / 256) consecutive elements per thread.
 // Dynamic shared memory, 24 bytes per entry of a.smem_cap:
 //   classification: k1 v1 k2 v2 (sort buffers), row ids, packed values;
-//   regression:     k1 v1 k2 v2, fixed-point targets (8 bytes).
+//   regression:     k1 v1 k2 v2, packed (target, weight) words (8 bytes).
 template <int CW, int SMEM_CAP>
 __global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(LevelArgs a) {
   __shared__ SortSmem<kBigBlock> SS;
@@ -712,7 +754,9 @@ __global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(Lev
         s_pv[i] = ((uint32_t)__ldg(P.lab + row) << 27) | (uint32_t)(wts ? __ldg(wts + i) : 1);
       }
     } else {
-      for (int i = threadIdx.x; i < m; i += kBigBlock) q_e[i] = __ldg(P.q + __ldg(rows + i));
+      const int wb = qw_bits(P.N);
+      for (int i = threadIdx.x; i < m; i += kBigBlock)
+        q_e[i] = qw_pack(__ldg(P.q + __ldg(rows + i)), wts ? __ldg(wts + i) : 1, wb);
     }
     if (threadIdx.x == 0 && packed)
       s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
@@ -768,10 +812,16 @@ __global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(Lev
       const uint32_t* sv = in2 ? v2 : v1;
       float g;
       int p;
-      long long nl, sl;
+      long long nl, sl = 0;
       unsigned long long L[CW];
-      big_boundary<CW, false>(sk, sv, packed, wts, q_e, m, per, nd, P, ncnt, a.H, s_prior,
-                       scan64, &g, &p, &nl, &sl, L);
+      if (packed) {
+        big_boundary<CW, false>(sk, sv, m, per, nd, P, ncnt, a.H, s_prior, scan64, &g, &p, &nl, L);
+      } else {
+        big_boundary_reg(sk, sv, q_e, m, per, nd.n, nd.sum, max(1, P.min_leaf), P.S, P.N, scan64,
+                         &g, &p, &nl, &sl);
+#pragma unroll
+        for (int c = 0; c < CW; ++c) L[c] = 0;
+      }
       const int bp = block_best_pos<kBigBlock>(g, p, s_g, s_p);
       if (bp >= 0 && p == bp) {
         Cand c;

@@ -265,6 +265,45 @@ __device__ __forceinline__ float variance_gain(long long nL, long long SL, long 
   return scale_pow2(g, -2 * S);
 }
 
+// Bounds lo <= variance_gain(nL, SL, nR, SR, S) <= hi from a few float
+// operations, so that a scan evaluates the float-float gain only where it can
+// reach the best.  With a = float(nL), b = float(nR) (the values variance_gain
+// divides by), the mean difference is (SL b - SR a) / (a b); its float
+// numerator is within 3.001 * 2^-24 * A of the exact one, A = |SL| b + |SR| a,
+// and variance_gain's own difference within 2^-43 A / (a b).  The margin
+// e = 2^-20 A covers both and __fdividef's 2 ulp; the last factor 1 +- 2^-16
+// covers the remaining roundings (a dozen at 2^-24 each).  rc = 1 / float(n)
+// rounded, p2 = 2^(-2S) (-2S in [-124, 120]: one exact scaling, monotone as in
+// variance_gain).  No overflow: a side's mean is at most 2^(61 - ceil(log2 N))
+// in magnitude, so hi stays below 2^128.  Requires nL, nR >= 1.
+__device__ __forceinline__ void variance_gain_bounds(int nL, long long SL, int nR, long long SR,
+                                                     float rc, float p2, float& lo, float& hi) {
+  const float a = __int2float_rn(nL), b = __int2float_rn(nR);
+  const float t1 = __fmul_rn(__ll2float_rn(SL), b);
+  const float t2 = __fmul_rn(__ll2float_rn(SR), a);
+  const float d = fabsf(__fsub_rn(t1, t2));
+  const float e = __fmul_rn(__fadd_rn(fabsf(t1), fabsf(t2)), 0x1p-20f);
+  const float ab = __fmul_rn(a, b);
+  const float w = __fmul_rn(ab, rc);
+  const float du = __fdividef(__fadd_rn(d, e), ab);
+  const float dl = __fdividef(fmaxf(__fsub_rn(d, e), 0.0f), ab);
+  hi = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(du, du), w), 0x1.0001p0f), p2);
+  lo = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(dl, dl), w), 0x1.fffep-1f), p2);
+}
+
+// A regression entry's fixed-point target q and weight w in one word,
+// q * 2^wb + w with wb the bit length of N.  Lossless: a tree draws N rows, so
+// 0 <= w <= N < 2^wb, and the target scale keeps |q| <= 2^(61 - ceil(log2 N))
+// <= 2^(62 - wb), so |q * 2^wb| <= 2^62.
+__device__ __forceinline__ int qw_bits(long long N) { return 64 - __clzll(N); }
+__device__ __forceinline__ long long qw_pack(long long q, int w, int wb) {
+  return q * (1ll << wb) + w;
+}
+__device__ __forceinline__ int qw_weight(long long x, int wb) {
+  return (int)(x & ((1ll << wb) - 1));
+}
+__device__ __forceinline__ long long qw_target(long long x, int wb) { return x >> wb; }
+
 // Walks trees t0 .. t0+W-1 for one row in lockstep, so that W independent
 // node loads are in flight at a time; x(f) reads the row's value of feature f.
 // leaf[k] receives tree t0+k's leaf (predict layout, PNode).
