@@ -400,10 +400,11 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, int m, int 
 // thread per tile as above.  Out of line, so that its registers do not weigh
 // on the classification scan of the same kernels.  The float-float gain is
 // evaluated only at boundaries whose upper bound (variance_gain_bounds)
-// reaches t, the larger of the best gain so far and the lower bounds of the
-// thread's boundaries in the tile: a boundary below t can neither be nor tie
-// the best.  n, sum: the node's weight and weighted target sum; S: the target
-// scale; N: the problem's rows (the packing).
+// reaches t, the largest over the warp of the lanes' best gains so far and of
+// the lower bounds of their boundaries in the tile: a boundary below t can
+// neither be nor tie the block's best.  n, sum: the node's weight and
+// weighted target sum; S: the target scale; N: the problem's rows (the
+// packing).
 static __device__ __noinline__ void big_boundary_reg(const uint32_t* sk, const uint32_t* sv,
                                                      const long long* eq, int m, int per,
                                                      long long n, long long sum, int ml, int S,
@@ -467,6 +468,8 @@ static __device__ __noinline__ void big_boundary_reg(const uint32_t* sk, const u
         rs += q[j];
       }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(kFull, t, o));
 #pragma unroll
     for (int j = 0; j < kBigPer; ++j) {
       if (((cand >> j) & 1u) && hi[j] >= t) {

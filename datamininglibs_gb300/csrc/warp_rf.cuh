@@ -90,6 +90,88 @@ constexpr int warp_rf_min_blocks() {
   return 16 / warp_rf_wpb<E>();
 }
 
+struct RegScan {
+  float g;    // the lane's best gain, -FLT_MAX if none
+  int p;      // its sorted position, -1 if none
+  long long nl, sl;  // left weight and weighted target sum there
+};
+
+// Regression boundary scan of one sorted try of a warp kernel: lane l owns
+// sorted positions p0 = l*E .. p0+E-1, its keys at sk[0 .. E-1] (key, entry
+// index) and prevk the key before them; sw / sqw: the entries' weights and
+// fixed-point targets.  One warp scan of the lanes' weights and target sums,
+// then each lane walks its positions.  The float-float gain is evaluated only
+// where variance_gain_bounds' upper bound reaches the largest lower bound over
+// the warp: a boundary below it can neither be nor tie the warp's best.
+// n, sum: the node's weight and weighted target sum; S: the target scale.
+template <int E>
+static __device__ __forceinline__ RegScan warp_reg_scan(const unsigned long long* sk,
+                                                        uint32_t prevk, int p0, const int* sw,
+                                                        const long long* sqw, long long n,
+                                                        long long sum, int ml, int S) {
+  const float rc = __frcp_rn(__ll2float_rn(n));
+  const float p2 = pow2f(-2 * S);
+  long long tn = 0, ts = 0;
+  unsigned bnd = 0;  // bit j: position p0 + j starts a new key
+#pragma unroll 1
+  for (int j = 0; j < E; ++j) {
+    const unsigned long long kv = sk[j];
+    if (kv == ~0ull) break;
+    const int e = (int)(kv & 0xFFFFFFFFull);
+    const uint32_t kk = (uint32_t)(kv >> 32);
+    if (p0 + j > 0 && prevk < kk) bnd |= 1u << j;
+    prevk = kk;
+    const int w = sw[e];
+    tn += w;
+    ts += sqw[e] * (long long)w;
+  }
+  const long long nl0 = warp_excl_scan<long long>(tn);
+  const long long sl0 = warp_excl_scan<long long>(ts);
+  float t = -FLT_MAX;
+  {
+    long long nl = nl0, sl = sl0;
+#pragma unroll 1
+    for (int j = 0; j < E && bnd >> j; ++j) {
+      const int e = (int)(sk[j] & 0xFFFFFFFFull);
+      const int w = sw[e];
+      const long long nr = n - nl;
+      if (((bnd >> j) & 1u) && nl >= ml && nr >= ml) {
+        float lo, hi;
+        variance_gain_bounds((int)nl, sl, (int)nr, sum - sl, rc, p2, lo, hi);
+        t = fmaxf(t, lo);
+      }
+      sl += sqw[e] * (long long)w;
+      nl += w;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(kFull, t, o));
+  RegScan r{-FLT_MAX, -1, 0, 0};
+  long long nl = nl0, sl = sl0;
+#pragma unroll 1
+  for (int j = 0; j < E && bnd >> j; ++j) {
+    const int e = (int)(sk[j] & 0xFFFFFFFFull);
+    const int w = sw[e];
+    const long long nr = n - nl;
+    if (((bnd >> j) & 1u) && nl >= ml && nr >= ml) {
+      float lo, hi;
+      variance_gain_bounds((int)nl, sl, (int)nr, sum - sl, rc, p2, lo, hi);
+      if (hi >= t) {
+        const float g = variance_gain(nl, sl, nr, sum - sl, S);
+        if (r.p < 0 || g > r.g) {
+          r.g = g;
+          r.p = p0 + j;
+          r.nl = nl;
+          r.sl = sl;
+        }
+      }
+    }
+    sl += sqw[e] * (long long)w;
+    nl += w;
+  }
+  return r;
+}
+
 template <int E, int CW>
 __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>())
     k_warp_rf(LevelArgs a) {
@@ -245,47 +327,15 @@ __global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>()
         bg = nb.gain(nd.n);
         bp = nb.p;
       } else {
-        // regression: lane l owns sorted positions l*E .. l*E+E-1; one warp
-        // scan of the lanes' row counts and target sums, then each lane walks
-        // its positions (rolled loops re-reading shared memory)
+        // regression: lane l owns sorted positions l*E .. l*E+E-1
         const int p0 = lane * E;
-        const unsigned long long* sk = &s_key[wb][p0 + lane];
-        long long tn = 0, ts = 0;
-        unsigned bnd = 0;  // bit j: position p0 + j starts a new key
-        uint32_t prevk =
-            p0 > 0 ? (uint32_t)(s_key[wb][p0 - 1 + (p0 - 1) / E] >> 32) : 0u;
-#pragma unroll 1
-        for (int j = 0; j < E; ++j) {
-          const unsigned long long kv = sk[j];
-          if (kv == ~0ull) break;
-          const int e = (int)(kv & 0xFFFFFFFFull);
-          const uint32_t kk = (uint32_t)(kv >> 32);
-          if (p0 + j > 0 && prevk < kk) bnd |= 1u << j;
-          prevk = kk;
-          const int w = s_w[wb][e];
-          tn += w;
-          ts += s_q_w[e] * (long long)w;
-        }
-        long long nl = warp_excl_scan<long long>(tn);
-        long long sl = warp_excl_scan<long long>(ts);
-#pragma unroll 1
-        for (int j = 0; j < E && bnd >> j; ++j) {
-          const unsigned long long kv = sk[j];
-          const int e = (int)(kv & 0xFFFFFFFFull);
-          const int w = s_w[wb][e];
-          const long long nr = (long long)nd.n - nl;
-          if (((bnd >> j) & 1u) && nl >= ml && nr >= ml) {
-            const float g = variance_gain(nl, sl, nr, nd.sum - sl, P.S);
-            if (bp < 0 || g > bg) {
-              bg = g;
-              bp = p0 + j;
-              my_nl = nl;
-              my_sl = sl;
-            }
-          }
-          sl += s_q_w[e] * (long long)w;
-          nl += w;
-        }
+        const RegScan rs = warp_reg_scan<E>(
+            &s_key[wb][p0 + lane], p0 > 0 ? (uint32_t)(s_key[wb][p0 - 1 + (p0 - 1) / E] >> 32) : 0u,
+            p0, s_w[wb], s_q_w, nd.n, nd.sum, ml, P.S);
+        bg = rs.g;
+        bp = rs.p;
+        my_nl = rs.nl;
+        my_sl = rs.sl;
       }
       // warp argmax: higher gain, then lower position
       float wg = bg;

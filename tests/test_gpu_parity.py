@@ -221,6 +221,27 @@ def test_regression_negative_and_tiny_targets(dml):
         assert np.array_equal(pg, po)
 
 
+@pytest.mark.parametrize("kind", ["discrete", "overflow", "large", "tiny"])
+def test_regression_big_nodes_tied_and_extreme_targets(dml, kind):
+    """Regression nodes above the shared-memory cap (the bounded boundary scan
+    of the big items): targets of four values over features of 20 values make
+    many exactly tied gains; targets near 1e30 make every gain +inf (ties at
+    infinity), near 1e13 large finite gains, near 1e-12 gains near 1e-21 with
+    the target scale at its upper clamp."""
+    X, y = synth.rf_regression(7000, 6, seed=91)
+    rng = np.random.default_rng(5)
+    if kind == "discrete":
+        X = (np.floor(X * 20.0) / 20.0).astype(np.float32)
+        y = rng.integers(0, 4, size=y.shape[0]).astype(np.float32)
+    else:
+        scale = {"overflow": 3e29, "large": 3e12, "tiny": 1e-12}[kind]
+        y = (y * np.float32(scale)).astype(np.float32)
+    kw = dict(algo=0, task=1, n_trees=3, K=3, max_depth=9, min_node_size=5, min_leaf=2, seed=4)
+    m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+    _assert_same_model(m, nodes, probs, kind)
+    assert np.array_equal(f.predict(X), oracle.predict(m, X))
+
+
 def test_invalid_inputs_rejected(dml):
     X, y = synth.ert_binary(200, 5, seed=1)
     Xn = X.copy()
