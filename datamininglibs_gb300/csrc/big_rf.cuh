@@ -395,6 +395,21 @@ __device__ void big_boundary(const uint32_t* sk, const uint32_t* sv, int m, int 
   for (int c = 0; c < CW; ++c) outL[c] = bL[c];
 }
 
+// The big items' classification scan, out of line: the sort's registers and
+// the scan's are allocated separately (the shared-memory kernel, whose sort
+// state is smaller, is faster with the scan inlined).
+template <int CW>
+static __device__ __noinline__ void big_boundary_items(const uint32_t* sk, const uint32_t* sv,
+                                                       int m, const LNode& nd, const ProbDesc& P,
+                                                       const int* ncnt, const long long* H,
+                                                       long long prior,
+                                                       unsigned long long* scan64, float* out_g,
+                                                       int* out_p, long long* out_nl,
+                                                       unsigned long long (&outL)[CW]) {
+  big_boundary<CW, true>(sk, sv, m, kBigPer, nd, P, ncnt, H, prior, scan64, out_g, out_p, out_nl,
+                         outL);
+}
+
 // Boundary scan of a sorted regression item, whose values index eq, the
 // entries' packed (target, weight) words; `per` (1..8) consecutive elements a
 // thread per tile as above.  Out of line, so that its registers do not weigh
@@ -586,8 +601,7 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     long long nl, sl = 0;
     unsigned long long L[CW];
     if (packed) {
-      big_boundary<CW, true>(sk, sv, m, kBigPer, nd, P, ncnt, a.H, s_prior, S.scan64, &g, &p, &nl,
-                             L);
+      big_boundary_items<CW>(sk, sv, m, nd, P, ncnt, a.H, s_prior, S.scan64, &g, &p, &nl, L);
     } else {
       big_boundary_reg(sk, sv, b.pq + nd.ebeg, m, kBigPer, nd.n, nd.sum, max(1, P.min_leaf), P.S,
                        P.N, S.scan64, &g, &p, &nl, &sl);
