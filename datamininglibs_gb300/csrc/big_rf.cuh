@@ -8,8 +8,11 @@
 // reordered in shared memory so that every digit's run is written to global
 // memory as one contiguous stretch.  The boundary scan gives each thread 8
 // consecutive sorted elements (one block scan of packed class counts per 2048
-// elements) and keeps the entropy incrementally.  A second kernel applies the
-// try loop (gpurf.cu:177-245) per node and partitions its entries.  The
+// elements) and keeps the entropy incrementally; a regression item's scan
+// reads one packed (target, weight) word per element and evaluates the
+// float-float variance gain only where its bound reaches the warp's best.
+// Both scans run out of line from the sort.  A second kernel applies the try
+// loop (gpurf.cu:177-245) per node and partitions its entries.  The
 // shared-memory kernel for mid-size nodes (k_rf_smem) is at the end.
 #pragma once
 #include "fit_kernels.cuh"
