@@ -104,6 +104,26 @@ def test_batched_uneven_forests_match_single_fits(dml):
         _assert_same_model(m, nodes, pr)
 
 
+def test_batched_regression_big_nodes_beside_ten_classes(dml):
+    """A regression problem with nodes above the shared-memory cap fitted in
+    one batch with a 10-class problem: the regression scans run in the kernels
+    of the widest class word and give each problem the oracle's forest."""
+    Xc, yc = synth.rf_multiclass(3000, 10, n_classes=10, n_int=3, seed=71)
+    Xr, yr = synth.rf_regression(7000, 6, seed=72)
+    specs = [dict(X=Xc, y=yc, algo=0, n_trees=3, K=3, max_depth=10, min_node_size=5,
+                  n_classes=10, seed=73),
+             dict(X=Xr, y=yr, algo=0, task=1, n_trees=3, K=3, max_depth=9, min_node_size=5,
+                  min_leaf=2, seed=74)]
+    batch = dml.fit_batched(specs)
+    for sp, fb in zip(specs, batch):
+        sp = dict(sp)
+        X, y = sp.pop("X"), sp.pop("y")
+        m = oracle.fit(X, y, **sp)
+        nodes, pr = fb.export()
+        _assert_same_model(m, nodes, pr)
+        assert np.array_equal(fb.predict(X), oracle.predict(m, X))
+
+
 def test_forests_of_one_fit_free_independently(dml):
     """The forests of one fit share one device allocation: each stays whole
     (export and predict equal the oracle's) while the others are freed in any
