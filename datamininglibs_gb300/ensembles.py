@@ -201,11 +201,20 @@ class Forest:
         _check(lib().dml_forest_info_get(self._h, ctypes.byref(i)))
         return i
 
-    def export(self):
-        """(nodes int32 [n, 5] in the Classify layout, probs float32)."""
+    def export(self, nodes=None, probs=None):
+        """(nodes int32 [n, 5] in the Classify layout, probs float32), written
+        into the given host arrays when passed (e.g. pinned buffers reused
+        across fits; their shapes must match the forest's)."""
         i = self.info()
-        nodes = np.zeros((i.n_nodes, 5), np.int32)
-        probs = np.zeros(i.n_probs, np.float32)
+        if nodes is None:
+            nodes = np.zeros((i.n_nodes, 5), np.int32)
+        if probs is None:
+            probs = np.zeros(i.n_probs, np.float32)
+        if (nodes.shape != (i.n_nodes, 5) or nodes.dtype != np.int32 or probs.shape != (i.n_probs,)
+                or probs.dtype != np.float32 or not nodes.flags.c_contiguous
+                or not probs.flags.c_contiguous):
+            raise ValueError("export buffers must be int32 [%d, 5] and float32 [%d], contiguous"
+                             % (i.n_nodes, i.n_probs))
         _check(lib().dml_forest_export(self._h, nodes.ctypes.data, probs.ctypes.data))
         return nodes, probs
 

@@ -124,6 +124,20 @@ def test_batched_regression_big_nodes_beside_ten_classes(dml):
         assert np.array_equal(fb.predict(X), oracle.predict(m, X))
 
 
+def test_export_into_given_buffers(dml):
+    X, y = synth.ert_binary(800, 8, seed=3)
+    f = dml.fit(X, y, algo=1, n_trees=3, K=3, max_depth=8, n_classes=2, seed=1)
+    nodes, probs = f.export()
+    n2, p2 = np.full_like(nodes, -7), np.full_like(probs, -7.0)
+    out = f.export(n2, p2)
+    assert out[0] is n2 and out[1] is p2
+    assert np.array_equal(n2, nodes) and np.array_equal(p2, probs)
+    with pytest.raises(ValueError):
+        f.export(n2[:-1], p2)
+    with pytest.raises(ValueError):
+        f.export(n2, p2.astype(np.float64))
+
+
 def test_forests_of_one_fit_free_independently(dml):
     """The forests of one fit share one device allocation: each stays whole
     (export and predict equal the oracle's) while the others are freed in any
