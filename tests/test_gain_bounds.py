@@ -92,3 +92,18 @@ def test_variance_gain_bounds_hold(seed):
     width = (hi[sel].astype(np.float64) - lo[sel]) / g[sel]
     assert sel.sum() > 500 and np.median(width) < 2.0 ** -13
     assert (width < 2.0 ** -10).mean() > 0.98
+
+
+def test_target_weight_packing_is_lossless():
+    """qw_pack (csrc/dml_device.cuh): q * 2^wb + w in an int64, wb the bit
+    length of N, for every weight 0..N a tree can give an entry and every
+    target the scale allows, |q| <= 2^(61 - ceil(log2 N)); unpacked by the
+    low wb bits and an arithmetic shift."""
+    for N in [2, 3, 4, 5, 4601, 1 << 16, (1 << 16) + 1, 1_000_000, 4_000_000, (1 << 27) - 1]:
+        wb = N.bit_length()
+        qmax = 2 ** (61 - (N - 1).bit_length())
+        for q in (qmax, -qmax, qmax - 1, -qmax + 1, 0, 1, -1):
+            for w in (0, 1, 2, N - 1, N):
+                x = q * (1 << wb) + w
+                assert -(1 << 63) <= x < (1 << 63)
+                assert x & ((1 << wb) - 1) == w and x >> wb == q
