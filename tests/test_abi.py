@@ -84,3 +84,41 @@ def test_server_config_checked_before_device_work(lib):
                 e.ServerConfig(1 << 30, 1024, 0, 0, 0), e.ServerConfig(1 << 30, 1024, 2, -1, 0),
                 e.ServerConfig(1 << 30, 1024, 2, 0, -5)):
         assert lib.dml_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+
+
+def test_forest_import_structure_checked_before_device_work(lib):
+    """dml_forest_import refuses on the host a node array whose internal nodes
+    do not point forward to an adjacent child pair inside the array (the
+    guarantee that a predict walk ends), whose split attribute is out of
+    range, or whose leaves point outside the probability array."""
+    def imp(nodes, probs, n_trees=1, n_classes=2, n_features=3, task=0):
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        probs = np.ascontiguousarray(probs, np.float32)
+        h = ctypes.c_void_p()
+        return lib.dml_forest_import(task, n_trees, n_classes, n_features, nodes.ctypes.data,
+                                     len(nodes), probs.ctypes.data, len(probs), ctypes.byref(h))
+
+    thr = int(np.array([0.5], np.float32).view(np.int32)[0])
+    leaf = [-1, 0, 0, -1, -1]       # child_start, child_count, prob_start, attribute, split
+    probs = np.array([1, 0, 0, 1], np.float32)
+
+    def split(child, attr=0, count=2):
+        return [child, count, -1, attr, thr]
+
+    cases = {
+        "child points backward (a cycle)": [split(0), leaf, [-1, 0, 2, -1, -1]],
+        "child pair runs past the array": [split(2), leaf, [-1, 0, 2, -1, -1]],
+        "one child": [split(1, count=1), leaf, [-1, 0, 2, -1, -1]],
+        "attribute out of range": [split(1, attr=3), leaf, [-1, 0, 2, -1, -1]],
+        "negative attribute": [split(1, attr=-2), leaf, [-1, 0, 2, -1, -1]],
+        "leaf past the probabilities": [split(1), leaf, [-1, 0, 3, -1, -1]],
+        "leaf before the probabilities": [split(1), leaf, [-1, 0, -1, -1, -1]],
+    }
+    for what, nodes in cases.items():
+        assert imp(nodes, probs) == 1, what
+        assert b"malformed" in lib.dml_last_error() or b"outside" in lib.dml_last_error(), what
+    # bad arguments: fewer nodes than trees, unknown task, classes out of range
+    ok_nodes = [split(1), leaf, [-1, 0, 2, -1, -1]]
+    assert imp(ok_nodes, probs, n_trees=4) == 1
+    assert imp(ok_nodes, probs, task=7) == 1
+    assert imp(ok_nodes, probs, n_classes=0) == 1
