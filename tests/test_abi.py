@@ -122,3 +122,33 @@ def test_forest_import_structure_checked_before_device_work(lib):
     assert imp(ok_nodes, probs, n_trees=4) == 1
     assert imp(ok_nodes, probs, task=7) == 1
     assert imp(ok_nodes, probs, n_classes=0) == 1
+
+
+def test_fit_descriptors_checked_before_device_work(lib):
+    """dml_fit and dml_fit_batched refuse bad descriptors on the host with
+    DML_ERR_INVALID_ARG and a message naming the forest, before any device
+    work (so this runs without a GPU)."""
+    from datamininglibs_gb300 import ensembles as e
+    X = np.zeros((4, 100), np.float32)
+    y = np.zeros(100, np.float32)
+
+    def desc(**kw):
+        p = dict(algo=0, task=0, n_trees=2, K=0, max_depth=10, min_node_size=5, min_leaf=1,
+                 n_classes=2, seed=0, balanced=0)
+        p.update(kw)
+        return e._desc(X, y, p["algo"], p["task"], p["n_trees"], p["K"], p["max_depth"],
+                       p["min_node_size"], p["min_leaf"], p["n_classes"], p["seed"], 0,
+                       p["balanced"])
+
+    bad = [dict(n_trees=0), dict(n_classes=0), dict(n_classes=33), dict(algo=5), dict(task=3),
+           dict(task=1, balanced=1), dict(algo=1, balanced=1), dict(max_depth=-1), dict(K=-1),
+           dict(min_node_size=-1)]
+    h = ctypes.c_void_p()
+    for kw in bad:
+        d = desc(**kw)
+        assert lib.dml_fit(ctypes.byref(d), ctypes.byref(h), None) == 1, kw
+        assert lib.dml_last_error().startswith(b"forest 0:"), kw
+    arr = (e.FitDesc * 3)(desc(), desc(n_classes=2), desc(algo=7))
+    outs = (ctypes.c_void_p * 3)()
+    assert lib.dml_fit_batched(3, arr, outs, None) == 1
+    assert lib.dml_last_error().startswith(b"forest 2:")
