@@ -3,6 +3,8 @@
 // (lib_ensembles/test/test_gpurf.h, test_gpuert.h).  Modes:
 //   parse <in.csv> <out.bin>   ParsingInterface::ParseFile<float>, dumped
 //   fit <data.bin> <out_dir>   RF fit/predict, split + aggregate, double frames
+//   host                       host-only parts: param packs, SplitParameterPack,
+//                              SplitModel / AggregateModels (no GPU needed)
 #include <datamininglibs.h>
 
 #include <cstdio>
@@ -45,9 +47,92 @@ static std::vector<int32_t> raw_nodes(const sp<lib_models::MlModel>& m) {
   return raw;
 }
 
+// The host-only parts of the algorithm API.  The model is three trees in the
+// layout AggregateModels writes (roots first, then each tree's child pairs in
+// depth-first order, leaves' probabilities in visiting order), so splitting
+// it and aggregating the parts must give it back exactly.
+static int host_checks() {
+  using Node = lib_ensembles::GpuDteAlgorithmShared::gpuDTE_NodeHeader_Classify<float>;
+  auto& ens = EnsemblesLib::GetInstance();
+  for (int e = 0; e < 2; ++e) {  // ensembles_interface.cc:28-58
+    auto p = e ? ens.CreateGpuErtParamPack() : ens.CreateGpuRfParamPack();
+    CHECK(p->Get<int>(EnsemblesLib::kNrTrees) == 100);
+    CHECK(p->Get<int>(EnsemblesLib::kNrFeatures) == 0);
+    CHECK(p->Get<int>(EnsemblesLib::kMaxDepth) == 1000);
+    CHECK(p->Get<int>(EnsemblesLib::kMinNodeSize) == 5);
+    CHECK(p->Get<AlgorithmsLib::AlgorithmType>(EnsemblesLib::kAlgoType) ==
+          AlgorithmsLib::kClassification);
+    CHECK(p->Get<bool>(EnsemblesLib::kBagging) == (e == 0));
+    CHECK(!p->Get<bool>(EnsemblesLib::kEasyEnsemble));
+  }
+  // every user value survives the split (the reference rebuilt default packs)
+  auto rf = ens.CreateGpuRfAlgorithm<float>();
+  auto p = ens.CreateGpuRfParamPack();
+  p->Set(EnsemblesLib::kNrTrees, 10);
+  p->Set(EnsemblesLib::kNrFeatures, 5);
+  p->Set(EnsemblesLib::kMaxDepth, 7);
+  p->Set(EnsemblesLib::kMinNodeSize, 9);
+  p->Set(EnsemblesLib::kAlgoType, AlgorithmsLib::kRegression);
+  p->Set(EnsemblesLib::kMinLeaf, 3);
+  p->Set(EnsemblesLib::kSeed, 11);
+  auto packs = rf->SplitParameterPack(p, 3);
+  CHECK(packs.size() == 3);
+  const int want[3] = {4, 3, 3};
+  int off = 0;
+  for (int i = 0; i < 3; ++i) {
+    auto& q = packs[i];
+    CHECK(q->Get<int>(EnsemblesLib::kNrTrees) == want[i]);
+    CHECK(q->Get<int>(EnsemblesLib::kTreeOffset) == off);
+    CHECK(q->Get<int>(EnsemblesLib::kNrFeatures) == 5);
+    CHECK(q->Get<int>(EnsemblesLib::kMaxDepth) == 7);
+    CHECK(q->Get<int>(EnsemblesLib::kMinNodeSize) == 9);
+    CHECK(q->Get<AlgorithmsLib::AlgorithmType>(EnsemblesLib::kAlgoType) ==
+          AlgorithmsLib::kRegression);
+    CHECK(q->Get<int>(EnsemblesLib::kMinLeaf) == 3);
+    CHECK(q->Get<int>(EnsemblesLib::kSeed) == 11);
+    off += want[i];
+  }
+  CHECK(p->Get<int>(EnsemblesLib::kNrTrees) == 10);
+  // tree 0: a split with two leaves; tree 1: one leaf; tree 2: two levels
+  std::vector<Node> nodes = {
+      {3, 2, -1, 1, 0.5f},  {-1, 0, 4, -1, -1.0f}, {5, 2, -1, 0, 0.25f},
+      {-1, 0, 0, -1, -1.0f}, {-1, 0, 2, -1, -1.0f}, {7, 2, -1, 2, 0.75f},
+      {-1, 0, 10, -1, -1.0f}, {-1, 0, 6, -1, -1.0f}, {-1, 0, 8, -1, -1.0f}};
+  std::vector<float> probs = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
+  auto m = ModelsLib::GetInstance().CreateModel();
+  m->Add(ModelsLib::kNrTrees, 3);
+  m->Add(ModelsLib::kNrTargets, 2);
+  m->Add(ModelsLib::kNrFeatures, 4);
+  m->Add(ModelsLib::kModelType, AlgorithmsLib::kClassification);
+  m->Add(ModelsLib::kNodeArray, nodes);
+  m->Add(ModelsLib::kProbArray, probs);
+  for (int k = 1; k <= 3; ++k) {
+    auto parts = rf->SplitModel(m, k);
+    CHECK((int)parts.size() == k);
+    int trees = 0;
+    for (auto& q : parts) trees += q->Get<int>(ModelsLib::kNrTrees);
+    CHECK(trees == 3);
+    auto agg = rf->AggregateModels(parts);
+    CHECK(agg->Get<int>(ModelsLib::kNrTrees) == 3);
+    CHECK(agg->Get<int>(ModelsLib::kNrTargets) == 2);
+    CHECK(agg->Get<int>(ModelsLib::kNrFeatures) == 4);
+    CHECK(raw_nodes(agg) == raw_nodes(m));
+    CHECK(agg->Get<std::vector<float>>(ModelsLib::kProbArray) == probs);
+  }
+  // one tree per part: each part's root is its tree's root, children re-based
+  auto single = rf->SplitModel(m, 3);
+  CHECK(single[1]->Get<std::vector<Node>>(ModelsLib::kNodeArray).size() == 1);
+  CHECK(single[2]->Get<std::vector<Node>>(ModelsLib::kNodeArray)[0].child_start == 1);
+  CHECK(single[2]->Get<std::vector<float>>(ModelsLib::kProbArray).size() == 6);
+  std::cout << "host ok\n";
+  return 0;
+}
+
 int main(int argc, char** argv) {
-  if (argc < 4) return 2;
+  if (argc < 2) return 2;
   std::string mode = argv[1];
+  if (mode == "host") return host_checks();
+  if (argc < 4) return 2;
   auto& parser = ParsingLib::GetInstance();
   if (mode == "parse") {
     try {

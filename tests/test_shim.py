@@ -59,6 +59,15 @@ def test_csv_parser_rejects_ragged_rows(shim_test, tmp_path):
     assert r.returncode == 3
 
 
+def test_shim_host_parts(shim_test):
+    """Param-pack defaults, SplitParameterPack keeping every user value with
+    tree offsets, and SplitModel / AggregateModels round trips, all on the
+    host (no GPU)."""
+    r = subprocess.run([shim_test, "host"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "host ok" in r.stdout
+
+
 @pytest.mark.gpu
 def test_shim_fit_predict_split_aggregate(shim_test, tmp_path):
     from datamininglibs_gb300 import synth
