@@ -7,6 +7,7 @@
 //                              SplitModel / AggregateModels (no GPU needed)
 #include <datamininglibs.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -124,6 +125,18 @@ static int host_checks() {
   CHECK(single[1]->Get<std::vector<Node>>(ModelsLib::kNodeArray).size() == 1);
   CHECK(single[2]->Get<std::vector<Node>>(ModelsLib::kNodeArray)[0].child_start == 1);
   CHECK(single[2]->Get<std::vector<float>>(ModelsLib::kProbArray).size() == 6);
+  // votes of split predictions add up (AggregateResults); the accuracy rule
+  // takes the first class of the largest count, strictly greater than 0
+  // (ml_resultdata_impl.cc:17-71), so ties and all-zero rows go to class 0
+  auto r1 = DataLib::GetInstance().CreateResultData<float>();
+  auto r2 = DataLib::GetInstance().CreateResultData<float>();
+  r1->AddPredictions({{1, 1}, {0, 2}, {3, 1}, {0, 0}});
+  r2->AddPredictions({{0, 0}, {0, 1}, {0, 0}, {0, 0}});
+  auto sum = rf->AggregateResults({r1, r2});
+  const std::vector<std::vector<float>> want_votes = {{1, 1}, {0, 3}, {3, 1}, {0, 0}};
+  CHECK(sum->GetPredictions() == want_votes);
+  const float acc = sum->GetAccuracy({0, 1, 1, 0});
+  CHECK(std::abs(acc - 0.75f) < 1e-6f);
   std::cout << "host ok\n";
   return 0;
 }

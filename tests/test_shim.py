@@ -61,8 +61,8 @@ def test_csv_parser_rejects_ragged_rows(shim_test, tmp_path):
 
 def test_shim_host_parts(shim_test):
     """Param-pack defaults, SplitParameterPack keeping every user value with
-    tree offsets, and SplitModel / AggregateModels round trips, all on the
-    host (no GPU)."""
+    tree offsets, SplitModel / AggregateModels round trips, AggregateResults
+    and the accuracy rule, all on the host (no GPU)."""
     r = subprocess.run([shim_test, "host"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "host ok" in r.stdout
