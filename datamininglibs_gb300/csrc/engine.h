@@ -26,6 +26,8 @@ struct dml_forest {
   float* probs = nullptr;              // device
   long long n_probs = 0;
   dml::PNode* pnodes = nullptr;        // device, predict layout
+  float* gains = nullptr;              // device, FP32 gain per node (NaN for leaves); null
+                                       // for forests not fitted by this engine
   dml::ForestBlock* block = nullptr;   // set when the three arrays live in a shared block
   int max_depth = 0;
   double fit_ms = 0.0;

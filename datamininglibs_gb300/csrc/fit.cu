@@ -101,12 +101,18 @@ void dev_free(void* p, cudaStream_t s) {
 }
 
 // Keeps freed pool memory cached in this process so that repeated fits and
-// predictions reuse device buffers instead of returning to the driver.
+// predictions reuse device buffers instead of returning to the driver.  The
+// release threshold is an attribute of each device's own pool, so it is set
+// once per device (the first fit on it).
 void init_pool_once() {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
+  constexpr int kMaxDev = 64;
+  static std::once_flag once[kMaxDev];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
+    cudaGetLastError();
+    return;
+  }
+  std::call_once(once[dev], [dev] {
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
       uint64_t thr = UINT64_MAX;
@@ -307,6 +313,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
   DBuf<int2> parts;
   DBuf<int> qlist[kNumQ];
   DBuf<ClassifyNode> node_log;
+  DBuf<float> gain_log;
   DBuf<float> prob_log;
   DBuf<Seg> segs;
   DBuf<Cand> big_cand, big_partial;
@@ -327,6 +334,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     parts.release(s);
     for (auto& q : qlist) q.release(s);
     node_log.release(s);
+    gain_log.release(s);
     prob_log.release(s);
     segs.release(s);
     big_cand.release(s);
@@ -662,6 +670,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       res_nxt.reserve((size_t)2 * n, s, false);
       for (auto& q : qlist) q.reserve((size_t)2 * n, s, false);
       node_log.reserve((size_t)(log_base + n), s, true);
+      gain_log.reserve((size_t)(log_base + n), s, true);
       prob_log.reserve((size_t)(plog_base + n) * Cmax, s, true);
       segs.reserve((size_t)(depth + 1) * nprob, s, true);
       DML_CK(cudaMemsetAsync(segs.p + (size_t)depth * nprob, 0, sizeof(Seg) * nprob, s));
@@ -684,6 +693,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       e.log_base = log_base;
       e.plog_base = plog_base;
       e.node_log = node_log.p;
+      e.gain_log = gain_log.p;
       e.prob_log = prob_log.p;
       e.fbase_cur = fbase[depth & 1];
       e.lbase_cur = lbase[depth & 1];
@@ -784,11 +794,12 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       DML_CK(cudaMemcpyAsync(hseg.data(), segs.p, sizeof(Seg) * hseg.size(),
                              cudaMemcpyDeviceToHost, s));
     DML_CK(cudaStreamSynchronize(s));
-    // one block for every forest's node, probability and predict arrays
+    // one block for every forest's node, gain, probability and predict arrays
     auto al = [](long long b) { return (b + 255) & ~255ll; };
     long long block_bytes = 0;
     for (int i = 0; i < nprob; ++i)
       block_bytes += al(sizeof(ClassifyNode) * std::max<long long>(1, fnodes[i])) +
+                     al(sizeof(float) * std::max<long long>(1, fnodes[i])) +
                      al(sizeof(float) * std::max<long long>(1, fleaves[i] * hp[i].C)) +
                      al(sizeof(PNode) * std::max<long long>(1, fnodes[i]));
     ForestBlock* block = new ForestBlock();
@@ -815,12 +826,16 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       block->refs.fetch_add(1);
       f->nodes = (ClassifyNode*)bp;
       bp += al(sizeof(ClassifyNode) * std::max<long long>(1, f->n_nodes));
+      f->gains = (float*)bp;
+      bp += al(sizeof(float) * std::max<long long>(1, f->n_nodes));
       f->probs = (float*)bp;
       bp += al(sizeof(float) * std::max<long long>(1, f->n_probs));
       f->pnodes = (PNode*)bp;
       bp += al(sizeof(PNode) * std::max<long long>(1, f->n_nodes));
       if (nprob == 1) {
         DML_CK(cudaMemcpyAsync(f->nodes, node_log.p, sizeof(ClassifyNode) * f->n_nodes,
+                               cudaMemcpyDeviceToDevice, s));
+        DML_CK(cudaMemcpyAsync(f->gains, gain_log.p, sizeof(float) * f->n_nodes,
                                cudaMemcpyDeviceToDevice, s));
         DML_CK(cudaMemcpyAsync(f->probs, prob_log.p, sizeof(float) * f->n_probs,
                                cudaMemcpyDeviceToDevice, s));
@@ -835,6 +850,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           g.node_pos = sg.node_pos;
           g.node_cnt = sg.node_cnt;
           g.node_dst = f->nodes + no;
+          g.gain_dst = f->gains + no;
           g.leaf_rank = sg.leaf_rank;
           g.leaf_cnt = sg.leaf_cnt;
           g.C = hp[i].C;
@@ -849,8 +865,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       GatherSeg* d_gsegs = (GatherSeg*)alloc(sizeof(GatherSeg) * gsegs.size());
       DML_CK(cudaMemcpyAsync(d_gsegs, gsegs.data(), sizeof(GatherSeg) * gsegs.size(),
                              cudaMemcpyHostToDevice, s));
-      k_gather_segments<<<(unsigned)gsegs.size(), 256, 0, s>>>(d_gsegs, node_log.p, prob_log.p,
-                                                               Cmax);
+      k_gather_segments<<<(unsigned)gsegs.size(), 256, 0, s>>>(d_gsegs, node_log.p, gain_log.p,
+                                                               prob_log.p, Cmax);
       DML_CK(cudaGetLastError());
       ++st.launches;
     }
@@ -921,19 +937,24 @@ static dml_status fit_entry(const dml_fit_desc* descs, int n, dml_forest** out, 
 // ---------------------------------------------------------------------------
 // Allocation-free fit.
 //
-// For callers that cannot allocate device memory while they fit: code that
-// runs while its stream is being captured into a CUDA graph, a host process
-// whose device memory is owned by its own allocator or partitioned by a
-// budget, or a latency-critical service that must not take the implicit device
-// synchronisation of cudaMalloc / cudaFree.  Every working buffer of the fit
-// comes from one file-scope device array of kNaArenaBytes (about 20 MiB) that
-// every GPU which loads this library holds until the process exits; the model
-// is written to device buffers the caller owns.  The problem must fit the
-// array: at most kNaMaxRows rows, n_trees * n_rows <= kNaMaxSlots, at most
-// kNaMaxClasses classes.  All calls share the array, so calls whose work
-// overlaps on the GPU (other streams, other host threads) race: serialise
-// them.  The first call on a device looks up the array's device address with
-// that device current; make that first call before any stream capture.
+// For callers that cannot allocate device memory while they fit: a process
+// whose device memory is owned by its own allocator (a framework's caching
+// allocator, an arena sized at start-up) or partitioned by a budget, so that a
+// library allocating on its own would take memory nobody accounted for, and a
+// latency-critical service that keeps cudaMalloc / cudaFree (which can
+// synchronise the device and can fail under fragmentation) out of its steady
+// state.  Every working buffer of the fit comes from one file-scope device array
+// of kNaArenaBytes (about 20 MiB) that every GPU which loads this library holds
+// until the process exits; the model is written to device buffers the caller
+// owns.  The problem must fit the array: at most kNaMaxRows rows,
+// n_trees * n_rows <= kNaMaxSlots, at most kNaMaxClasses classes.  All calls
+// share the array and keep the last call's contents there (each call clears
+// what must start at zero), so calls whose work overlaps on the GPU (other
+// streams, other host threads) race: serialise them.  The call synchronises its
+// stream to read the validation result and then once per tree level (the next
+// level's size).  The first call on a device sets the array up with that device
+// current: it looks up the array's device address and uploads the n*ln(n) table
+// once.
 namespace dml {
 namespace noalloc {
 constexpr long long kNaMaxRows = 4096;
@@ -983,21 +1004,35 @@ namespace noalloc {
 constexpr int kMaxDevices = 64;
 static unsigned char* g_arena_dev[kMaxDevices];
 static std::mutex g_arena_mu;
-// host-side staging of the few values the driver reads back or uploads
-static long long g_h_table[kNaMaxRows + 1];
-static int g_h_tree_prob[kNaMaxSlots];
 
-// The array's device address on the current device (looked up once per device).
+// The array's device address on the current device, set up once per device:
+// cudaGetSymbolAddress with the device current (the array's name is only a
+// host-side stand-in), then the n*ln(n) table for every row count the array
+// admits (H[n] does not depend on the problem) uploaded to its slot.
 static unsigned char* arena_on_current_device() {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    set_error("no current CUDA device for the allocation-free fit");
+    return nullptr;
+  }
   std::lock_guard<std::mutex> lk(g_arena_mu);
   if (!g_arena_dev[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_arena);
     if (e != cudaSuccess) {
+      cudaGetLastError();
       set_error("cudaGetSymbolAddress of the allocation-free scratch failed: %s",
                 cudaGetErrorString(e));
+      return nullptr;
+    }
+    std::vector<long long> table((size_t)kNaMaxRows + 1);
+    build_nlogn_table(kNaMaxRows, table.data());
+    e = cudaMemcpy((unsigned char*)p + oH, table.data(), sizeof(long long) * table.size(),
+                   cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("upload of the allocation-free n*ln(n) table failed: %s", cudaGetErrorString(e));
       return nullptr;
     }
     g_arena_dev[dev] = (unsigned char*)p;
@@ -1017,7 +1052,7 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
   if ((d.algo != DML_ALGO_RF && d.algo != DML_ALGO_ERT) ||
       (d.task != DML_CLASSIFICATION && d.task != DML_REGRESSION) || d.n_trees <= 0 ||
       d.n_rows <= 0 || d.n_features <= 0 || !d.samples || !d.targets || d.max_depth < 0 ||
-      d.min_node_size < 0 || d.n_features_try < 0 ||
+      d.min_node_size < 0 || d.n_features_try < 0 || d.tree_offset < 0 ||
       (d.task == DML_CLASSIFICATION && d.n_classes < 1)) {
     set_error("invalid fit parameters");
     return DML_ERR_INVALID_ARG;
@@ -1109,19 +1144,13 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
         d.targets, P.N, P.task, P.S, P.lab == nullptr ? nullptr : (int*)(A + oLab),
         (long long*)(A + oQ));
     DML_CK(cudaGetLastError());
-    const long long* H = nullptr;
-    if (P.task == 0) {
-      build_nlogn_table(P.N, g_h_table);
-      DML_CK(cudaMemcpyAsync(A + oH, g_h_table, sizeof(long long) * (P.N + 1),
-                             cudaMemcpyHostToDevice, s));
-      H = (const long long*)(A + oH);
-    }
+    // the table was uploaded when the array was set up on this device
+    const long long* H = P.task == 0 ? (const long long*)(A + oH) : nullptr;
     ProbDesc* d_probs = (ProbDesc*)(A + oProb);
     DML_CK(cudaMemcpyAsync(d_probs, &P, sizeof(ProbDesc), cudaMemcpyHostToDevice, s));
-    for (int t = 0; t < d.n_trees; ++t) g_h_tree_prob[t] = 0;
+    // every tree belongs to problem 0
     int* d_tree_prob = (int*)(A + oTreeProb);
-    DML_CK(cudaMemcpyAsync(d_tree_prob, g_h_tree_prob, sizeof(int) * d.n_trees,
-                           cudaMemcpyHostToDevice, s));
+    DML_CK(cudaMemsetAsync(d_tree_prob, 0, sizeof(int) * d.n_trees, s));
     int* rowsA = (int*)(A + oRowsA);
     int* rowsB = (int*)(A + oRowsB);
     int* wA = d.algo == DML_ALGO_RF ? (int*)(A + oWA) : nullptr;
@@ -1219,6 +1248,7 @@ static dml_status run_fit_noalloc(const dml_fit_desc& d, ClassifyNode* nodes_out
       e.log_base = log_base;
       e.plog_base = plog_base;
       e.node_log = nodes_out;   // one forest: log order is the model order
+      e.gain_log = nullptr;
       e.prob_log = probs_out;   // Cmax == C: leaf payloads packed
       e.fbase_cur = fbase[depth & 1];
       e.lbase_cur = lbase[depth & 1];

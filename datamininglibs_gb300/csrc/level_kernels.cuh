@@ -525,6 +525,7 @@ struct EmitArgs {
   long long log_base;    // node log position of this level's first node
   long long plog_base;   // first leaf rank of this level in the probability log
   ClassifyNode* node_log;
+  float* gain_log;       // per node: the chosen split's FP32 gain, NaN for leaves (or null)
   float* prob_log;       // Cmax floats per leaf rank
   const long long* fbase_cur;
   const long long* lbase_cur;
@@ -610,6 +611,7 @@ __global__ void __launch_bounds__(256) k_emit(EmitArgs a) {
       }
     }
     a.node_log[a.log_base + j] = cn;
+    if (a.gain_log) a.gain_log[a.log_base + j] = r.split ? r.gain : __int_as_float(0x7FC00000);
     if (j == fs) {
       a.fbase_next[f] = fb + (fe - fs);
       a.lbase_next[f] = lb + (a.leafpos[fe] - a.leafpos[fs]);
@@ -710,14 +712,18 @@ __global__ void k_prep_all(const PrepJob* jobs) {
 struct GatherSeg {
   long long node_pos, leaf_rank, leaf_cnt;
   ClassifyNode* node_dst;
+  float* gain_dst;
   float* prob_dst;
   int node_cnt, C;
 };
 
 __global__ void k_gather_segments(const GatherSeg* segs, const ClassifyNode* log,
-                                  const float* plog, int Cmax) {
+                                  const float* glog, const float* plog, int Cmax) {
   const GatherSeg g = segs[blockIdx.x];
-  for (int i = threadIdx.x; i < g.node_cnt; i += blockDim.x) g.node_dst[i] = log[g.node_pos + i];
+  for (int i = threadIdx.x; i < g.node_cnt; i += blockDim.x) {
+    g.node_dst[i] = log[g.node_pos + i];
+    g.gain_dst[i] = glog[g.node_pos + i];
+  }
   const long long tot = g.leaf_cnt * g.C;
   for (long long i = threadIdx.x; i < tot; i += blockDim.x) {
     const long long l = i / g.C;

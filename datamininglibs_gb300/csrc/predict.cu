@@ -358,6 +358,28 @@ dml_status dml_forest_export(const dml_forest* f, void* node_array, float* probs
   return DML_OK;
 }
 
+dml_status dml_forest_gains(const dml_forest* f, float* gains, int32_t memory, void* stream) {
+  clear_error();
+  if (!f || (!gains && f->n_nodes) || (memory != DML_HOST && memory != DML_DEVICE)) {
+    set_error("null argument or bad memory kind");
+    return DML_ERR_INVALID_ARG;
+  }
+  if (!f->gains) {
+    set_error("the forest holds no split gains (it was imported or loaded, not fitted)");
+    return DML_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(gains, f->gains, sizeof(float) * f->n_nodes,
+                      memory == DML_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                      s) != cudaSuccess ||
+      (memory == DML_HOST && cudaStreamSynchronize(s) != cudaSuccess)) {
+    cudaGetLastError();
+    set_error("copy of the split gains failed");
+    return DML_ERR_CUDA;
+  }
+  return DML_OK;
+}
+
 dml_status dml_forest_import(int32_t task, int32_t n_trees, int32_t n_classes, int32_t n_features,
                              const void* node_array, int64_t n_nodes, const float* probs,
                              int64_t n_probs, dml_forest** out) {

@@ -1,8 +1,6 @@
 // Launch of the split-search kernels of one node class, instantiated per
 // packed class-count width CW in search_cw*.cu (compiled in parallel).
 #pragma once
-#include <mutex>
-
 #include "engine.h"
 #include "level_kernels.cuh"
 #include "big_rf.cuh"
@@ -20,13 +18,14 @@ template <int CW>
 void launch_big_cw(BigArgs b, int phase, int grid, int decide_grid, int tries, cudaStream_t s);
 
 #ifdef DML_SEARCH_CW
+// cudaFuncSetAttribute acts on the current device only, and fits run on
+// whatever device the calling thread selects, so the shared-memory limit of the
+// CTA kernel is raised before each of its launches (one per level, a host call
+// of about a microsecond) rather than once per process.
 template <int CW>
 static void set_smem_attrs() {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    cudaFuncSetAttribute(k_rf_smem<CW, kSmemCap>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kSmemCap * 24);
-  });
+  DML_CK(cudaFuncSetAttribute(k_rf_smem<CW, kSmemCap>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              kSmemCap * 24));
 }
 
 template <int CW>

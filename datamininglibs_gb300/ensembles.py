@@ -121,6 +121,8 @@ _SIGS = {
                                          ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
     "dml_forest_info_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForestInfo)]),
     "dml_forest_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dml_forest_gains": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                        ctypes.c_void_p]),
     "dml_forest_import": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                          ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
                                          ctypes.c_void_p, ctypes.c_int64,
@@ -217,6 +219,14 @@ class Forest:
                              % (i.n_nodes, i.n_probs))
         _check(lib().dml_forest_export(self._h, nodes.ctypes.data, probs.ctypes.data))
         return nodes, probs
+
+    def gains(self):
+        """float32 [n_nodes]: the FP32 gain of every node's chosen split as the
+        engine computed it on the device (NaN for leaves), in node-array order."""
+        i = self.info()
+        g = np.zeros(i.n_nodes, np.float32)
+        _check(lib().dml_forest_gains(self._h, g.ctypes.data, HOST, None))
+        return g
 
     def predict(self, X, out=None, stream=None):
         """X feature-major [F, N] (numpy or CUDA tensor).  Returns the

@@ -150,21 +150,26 @@ DML_API dml_status dml_fit_batched(int32_t n, const dml_fit_desc* descs, dml_for
 DML_API dml_status dml_fit_plain(const dml_fit_desc* desc, dml_forest** out, void* stream);
 
 /* No counterpart in the reference.  dml_fit for callers that cannot allocate
- * device memory while they fit (a stream being captured into a CUDA graph, a
- * process whose device memory belongs to its own allocator or budget, a
- * latency-critical service that must avoid the device synchronisation of
- * cudaMalloc/cudaFree).  Same trees as dml_fit.  It allocates nothing: its
- * working buffers live in one static device array of about 20 MiB that every
- * GPU loading this library holds until the process exits, so the problem must
- * fit it: at most 4096 rows, n_trees * n_rows <= 65536, at most 8 classes;
- * larger problems are rejected with DML_ERR_INVALID_ARG.  samples and targets
- * must be device pointers (desc->memory == DML_DEVICE).  The model is written
- * to caller-owned device buffers: node_array (Classify layout, 20 bytes per
- * node, room for n_trees * (2 * n_rows - 1) nodes) and probs (room for
- * n_trees * n_rows * n_classes floats); *n_nodes / *n_probs receive the sizes
- * used.  Calls share the static array: calls whose work overlaps on the GPU
- * race, so serialise them.  The first call on a device looks up the array's
- * address with that device current and should come before any stream capture. */
+ * device memory while they fit: a process whose device memory is owned by its
+ * own allocator (a framework's caching allocator, an arena sized at start-up)
+ * or partitioned by a budget, where memory a library allocates on its own is
+ * memory nobody accounted for; a latency-critical service that keeps
+ * cudaMalloc / cudaFree (which can synchronise the device and can fail under
+ * fragmentation) out of its steady state.  Same trees as dml_fit.  It
+ * allocates nothing: its working buffers live in one static device array of
+ * about 20 MiB that every GPU loading this library holds until the process
+ * exits, so the problem must fit it: at most 4096 rows, n_trees * n_rows <=
+ * 65536, at most 8 classes; larger problems are rejected with
+ * DML_ERR_INVALID_ARG.  samples and targets must be device pointers
+ * (desc->memory == DML_DEVICE).  The model is written to caller-owned device
+ * buffers: node_array (Classify layout, 20 bytes per node, room for
+ * n_trees * (2 * n_rows - 1) nodes) and probs (room for n_trees * n_rows *
+ * n_classes floats); *n_nodes / *n_probs receive the sizes used.  The call
+ * synchronises its stream once to read the data check and once per tree level.
+ * Calls share the static array, which keeps the last call's contents: calls
+ * whose work overlaps on the GPU race, so serialise them.  The first call on a
+ * device sets the array up with that device current (looks up its address and
+ * uploads a constant table). */
 DML_API dml_status dml_fit_noalloc(const dml_fit_desc* desc, void* node_array,
                                    int64_t node_capacity, float* probs, int64_t prob_capacity,
                                    int64_t* n_nodes, int64_t* n_probs, void* stream);
@@ -238,6 +243,18 @@ DML_API dml_status dml_forest_info_get(const dml_forest* forest, dml_forest_info
  * filled at gpudte_algorithm.cc:257-258).  node_array receives n_nodes * 20
  * bytes, probs n_probs floats (host memory). */
 DML_API dml_status dml_forest_export(const dml_forest* forest, void* node_array, float* probs);
+
+/* The FP32 information (or variance) gain of every node's chosen split, in
+ * kNodeArray order: n_nodes floats, NaN for leaves.  The reference computes
+ * these gains in its split search (entropy_over_columns -
+ * entropy_conditioned_on_rows, lib_ensembles/source/gpudte.cu:76-117;
+ * gpurf.cu:618-768, gpuert.cu:275-381) and keeps only the winning split, so it
+ * has no counterpart call.  memory says where `gains` lives (DML_HOST: the call
+ * returns when the copy is done; DML_DEVICE: ordered on `stream`).  Forests
+ * built by dml_forest_import / dml_forest_load hold no gains
+ * (DML_ERR_INVALID_ARG). */
+DML_API dml_status dml_forest_gains(const dml_forest* forest, float* gains, int32_t memory,
+                                    void* stream);
 
 /* A device-resident forest from kNodeArray / kProbArray in the layout above
  * (host memory), e.g. a model built by the reference or merged on the host. */

@@ -34,9 +34,10 @@
 //     (gpurf.cu:786-794)
 //   * regression leaf value = node mean (gpudte.cu:294-301)
 //   * gain ties broken by the lowest (feature, threshold)
-//   * entropy evaluated from an n*ln(n) table held as float pairs, so that the
-//     CPU and GPU produce identical FP32 gains; an independent FP64 gain is
-//     kept beside it for the tolerance check
+//   * entropy evaluated from an n*ln(n) table in int64 fixed point
+//     (round(n ln n * 2^28)), so that the gain numerators are exact integer
+//     sums and the CPU and GPU produce identical FP32 gains; an independent
+//     FP64 gain is kept beside it for the tolerance check
 //
 // Build: oracle/Makefile (g++ -O2 -fopenmp -ffp-contract=off).
 

@@ -2,9 +2,11 @@
 # sources where they lie: g++ on lib_ensembles/source/gpudte.cu (device code
 # compiled as host code through ref_shim/), and on the host-side sources of
 # lib_core, lib_data and lib_parsing.  The reference's own CMake build is not
-# used.  Output: oracle/_ref/libref.so (git-ignored).  Only runs where the
-# reference tree exists (REF).
-REF ?= /root/reference
+# used.  Output: oracle/_ref/libref.so (git-ignored).  REF names the reference
+# tree; oracle/ref.py passes it (from DML_REFERENCE_ROOT).
+ifndef REF
+$(error REF must name the reference source tree)
+endif
 OUT := _ref
 CXX ?= g++
 CXXFLAGS := -O1 -std=c++14 -fPIC -ffp-contract=off -w

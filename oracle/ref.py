@@ -12,6 +12,8 @@ import subprocess
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
+# The one place that says where the reference tree lies: DML_REFERENCE_ROOT, or
+# the checkout this project was built against.
 REF_ROOT = os.environ.get("DML_REFERENCE_ROOT", "/root/reference")
 _LIB = None
 

@@ -152,3 +152,37 @@ def test_fit_descriptors_checked_before_device_work(lib):
     outs = (ctypes.c_void_p * 3)()
     assert lib.dml_fit_batched(3, arr, outs, None) == 1
     assert lib.dml_last_error().startswith(b"forest 2:")
+
+
+def test_noalloc_descriptors_checked_before_device_work(lib):
+    """dml_fit_noalloc refuses, on the host and before it touches its device
+    array, what dml_fit refuses (a negative tree_offset included) and problems
+    larger than its array, with DML_ERR_INVALID_ARG."""
+    from datamininglibs_gb300 import ensembles as e
+    X = np.zeros((4, 100), np.float32)
+    y = np.zeros(100, np.float32)
+
+    def desc(tree_offset=0, n_rows=100, **kw):
+        p = dict(algo=0, task=0, n_trees=2, K=0, max_depth=10, min_node_size=5, min_leaf=1,
+                 n_classes=2, seed=0)
+        p.update(kw)
+        d = e._desc(X, y, p["algo"], p["task"], p["n_trees"], p["K"], p["max_depth"],
+                    p["min_node_size"], p["min_leaf"], p["n_classes"], p["seed"], tree_offset, 0)
+        d.memory = e.DEVICE  # never dereferenced: the checks come first
+        d.n_rows = n_rows
+        return d
+
+    nn, npb = ctypes.c_int64(), ctypes.c_int64()
+    fake = ctypes.c_void_p(4096)
+    bad = [dict(tree_offset=-1), dict(n_trees=0), dict(max_depth=-1), dict(K=-1),
+           dict(min_node_size=-1), dict(algo=4), dict(n_rows=4097), dict(n_classes=9),
+           dict(n_trees=700)]
+    for kw in bad:
+        d = desc(**kw)
+        assert lib.dml_fit_noalloc(ctypes.byref(d), fake, 1 << 30, fake, 1 << 30,
+                                   ctypes.byref(nn), ctypes.byref(npb), None) == 1, kw
+    host = desc()
+    host.memory = e.HOST
+    assert lib.dml_fit_noalloc(ctypes.byref(host), fake, 1 << 30, fake, 1 << 30, ctypes.byref(nn),
+                               ctypes.byref(npb), None) == 1
+    assert b"device pointers" in lib.dml_last_error()

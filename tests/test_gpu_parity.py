@@ -67,16 +67,47 @@ def test_fit_and_predict_bit_exact(dml, name):
     assert np.array_equal(pg, po), name
 
 
-def test_gains_within_tolerance_of_fp64(dml):
-    """FP32 gains of the chosen splits: the engine's equal the oracle's FP32
-    gains bit for bit (same trees), and those are within 1e-6 relative (plus
-    1e-7 absolute) of the FP64 gains."""
-    X, y = synth.rf_multiclass(3000, 16, n_classes=5, n_int=3, seed=21)
-    kw = dict(algo=0, n_trees=6, K=4, max_depth=14, min_node_size=5, n_classes=5, seed=2)
-    m = oracle.fit(X, y, **kw)
-    ok = ~np.isnan(m.gains32)
-    err = np.abs(m.gains32[ok].astype(np.float64) - m.gains64[ok])
-    assert np.all(err <= 1e-6 * np.abs(m.gains64[ok]) + 1e-7)
+GAIN_CASES = {
+    "ert_binary": (lambda: synth.ert_binary(2500, 57, seed=3),
+                   dict(algo=1, n_trees=16, K=7, max_depth=12, min_node_size=10, n_classes=2,
+                        seed=4)),
+    "rf_10_classes": (lambda: synth.rf_multiclass(20000, 32, n_classes=10, n_int=4, seed=21),
+                      dict(algo=0, n_trees=6, K=6, max_depth=20, min_node_size=5, min_leaf=2,
+                           n_classes=10, seed=2)),
+    "rf_regression": (lambda: synth.rf_regression(12000, 16, seed=22),
+                      dict(algo=0, task=1, n_trees=4, K=6, max_depth=24, min_node_size=5,
+                           min_leaf=5, seed=3)),
+    "ert_regression": (lambda: synth.rf_regression(3000, 12, seed=23),
+                       dict(algo=1, task=1, n_trees=6, K=4, max_depth=14, min_node_size=5,
+                            seed=4)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(GAIN_CASES))
+def test_gains_within_tolerance_of_fp64(dml, name):
+    """The FP32 gain of every split as the engine computed it on the device
+    (dml_forest_gains): bit for bit the oracle's FP32 gain, and within
+    1e-6 relative + 1e-7 absolute of the oracle's FP64 gain.  Leaves hold NaN."""
+    gen, kw = GAIN_CASES[name]
+    X, y = gen()
+    m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+    _assert_same_model(m, nodes, probs, name)
+    g = f.gains()
+    split = nodes[:, 1] > 0
+    assert split.any(), name
+    assert np.array_equal(np.isnan(g), ~split), name
+    assert np.array_equal(g[split].view(np.uint32), m.gains32[split].view(np.uint32)), name
+    err = np.abs(g[split].astype(np.float64) - m.gains64[split])
+    assert np.all(err <= 1e-6 * np.abs(m.gains64[split]) + 1e-7), (name, err.max())
+
+
+def test_imported_forest_has_no_gains(dml):
+    X, y = synth.ert_binary(600, 8, seed=5)
+    f = dml.fit(X, y, algo=1, n_trees=2, K=3, max_depth=6, n_classes=2, seed=1)
+    nodes, probs = f.export()
+    g = dml.Forest.from_model(nodes, probs, task=0, n_trees=2, n_classes=2, n_features=8)
+    with pytest.raises(dml.DmlError):
+        g.gains()
 
 
 def test_plain_path_matches_level_path(dml):

@@ -1,13 +1,15 @@
 """The allocation-free fit (dml_fit_noalloc) against dml_fit, through the C ABI.
 
 dml_fit_noalloc serves callers that cannot allocate device memory while they
-fit (a stream under CUDA-graph capture, a process whose device memory belongs to
-its own allocator, a service that must not take cudaMalloc's device
-synchronisation).  Its working buffers are one static device array shared by
-all calls, so each call here checks that stale contents left by the previous
-call do not leak into the next: two different fits in a row, each compared with
-dml_fit's model (trees and leaf counts bit-exact, as in the other parity tests).
-This file is collected last.
+fit: a process whose device memory belongs to its own allocator or budget, or a
+service that keeps cudaMalloc / cudaFree (device synchronisation, failures under
+fragmentation) out of its steady state.  Its working buffers are one static
+device array shared by all calls, which keeps the last call's contents, so each
+call here checks that stale contents left by the previous call do not leak into
+the next: different fits in a row, each compared with dml_fit's model (trees
+and leaf counts bit-exact, as in the other parity tests).  This file is
+collected last, so that a run stopping at the first failure has run every other
+test before it.
 """
 import numpy as np
 import pytest
