@@ -124,7 +124,7 @@ def traffic_from_profile(kernel):
     return None
 
 
-def cpu_baseline(w, X, y, threads, trees):
+def cpu_baseline(w, X, y, threads, trees, with_model=False):
     """The oracle (CPU restatement of the reference path) on all host threads,
     on the full-size data: ``trees`` of the workload's trees (one per thread
     when trees >= threads, otherwise the nodes of a level spread over threads)."""
@@ -135,9 +135,91 @@ def cpu_baseline(w, X, y, threads, trees):
     t0 = time.perf_counter()
     m = oracle.fit(X, y, threads=threads, **kw)
     dt = time.perf_counter() - t0
-    return {"value": m.nodes.shape[0] / dt, "unit": "nodes/s", "cores": threads,
-            "kind": "port", "sample": "%d of the %d trees on the full %dx%d data (%.1f s)" % (
-                trees, w["trees"], w["rows"], w["features"], dt)}
+    cb = {"value": m.nodes.shape[0] / dt, "unit": "nodes/s", "cores": threads,
+          "kind": "port", "sample": "%d of the %d trees on the full %dx%d data (%.1f s)" % (
+              trees, w["trees"], w["rows"], w["features"], dt)}
+    return (cb, m) if with_model else cb
+
+
+def oracle_rate(fn, what, threads):
+    """nodes/s of one oracle fit (all host threads) on a bounded sample."""
+    t0 = time.perf_counter()
+    nodes = fn()
+    dt = time.perf_counter() - t0
+    return {"value": nodes / dt, "unit": "nodes/s", "cores": threads, "kind": "port",
+            "sample": "%s (%.1f s)" % (what, dt)}
+
+
+def other_cpu_baselines(threads):
+    """The oracle on all host threads for the other workloads, each a bounded
+    sample of the workload on its full data (nodes/s)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from datamininglibs_gb300 import synth
+    out = {}
+    X1, y1 = synth.ert_binary()
+
+    def c1():
+        n = 0
+        for _ in range(5):
+            n += oracle.fit(X1, y1, algo=1, n_trees=64, K=7, max_depth=12, min_node_size=10,
+                            n_classes=2, seed=0, threads=threads).nodes.shape[0]
+        return n
+    out["ert_binary_4601x57_64trees"] = oracle_rate(c1, "5 fits of the whole 64-tree forest",
+                                                    threads)
+    probs = synth.uneven_problems(256, seed=0)
+
+    def c4():
+        return sum(oracle.fit(X, y, algo=1, n_trees=2, K=0, max_depth=16, min_node_size=5,
+                              n_classes=c, seed=i, threads=threads).nodes.shape[0]
+                   for i, (X, y, c) in enumerate(probs))
+    out["uneven_256_ert_forests"] = oracle_rate(
+        c4, "trees 0-1 of each of the 256 forests (16 trees each in the workload)", threads)
+    del probs
+    X3, y3 = synth.rf_regression()
+    X3 = np.ascontiguousarray(X3[:, :1_000_000])
+    y3 = np.ascontiguousarray(y3[:1_000_000])
+
+    def c3():
+        return oracle.fit(X3, y3, algo=0, task=1, n_trees=1, K=21, max_depth=24, min_node_size=5,
+                          min_leaf=5, seed=0, threads=threads).nodes.shape[0]
+    out["rf_regression_4Mx64_64trees"] = oracle_rate(
+        c3, "tree 0 of the 64 on the first 1,000,000 of the 4,000,000 rows (a tree on all "
+            "rows takes about 110 s on 16 Grace cores)", threads)
+    return out
+
+
+def parity_of_timed_forest(w, nodes, probs, gains, m):
+    """Trees 0.. of the timed forest against the oracle's fit of the same
+    workload's first trees (its cpu_baseline sample), tree by tree in
+    breadth-first form: structure, thresholds and leaf class counts bit for bit;
+    the engine's FP32 split gains bit for bit against the oracle's FP32 gains and
+    within 1e-6 relative + 1e-7 of its FP64 gains."""
+    from datamininglibs_gb300 import model
+    C = w["classes"]
+    exact = gains_exact = within = True
+    worst = 0.0
+    for t in range(m.n_trees):
+        en, ep, eg = model.tree_arrays(nodes, probs, C, t, gains)
+        on, op, og32 = model.tree_arrays(m.nodes, m.probs, C, t, m.gains32)
+        og64 = model.tree_arrays(m.nodes, m.probs, C, t, m.gains64)[2]
+        same = en.shape == on.shape and np.array_equal(en, on) and np.array_equal(ep, op)
+        exact = exact and same
+        if same:
+            sp = on[:, 1] > 0
+            gains_exact = gains_exact and np.array_equal(eg[sp].view(np.uint32),
+                                                         og32[sp].view(np.uint32))
+            err = np.abs(eg[sp].astype(np.float64) - og64[sp])
+            within = within and bool(np.all(err <= 1e-6 * np.abs(og64[sp]) + 1e-7))
+            big = np.abs(og64[sp]) > 1e-6
+            if big.any():
+                worst = max(worst, float((err[big] / np.abs(og64[sp][big])).max()))
+    return {"config": w["name"], "trees": m.n_trees, "bit_exact": bool(exact),
+            "gains_fp32_bit_exact": bool(gains_exact),
+            "gains_within_1e-6_rel_1e-7_abs_of_fp64": bool(within),
+            "gains_max_rel_err_vs_fp64": worst,
+            "compared": "trees 0..%d of the last timed %d-tree forest vs the oracle's "
+                        "cpu_baseline fit" % (m.n_trees - 1, w["trees"])}
 
 
 def run_reference(args, w):
@@ -260,28 +342,49 @@ def serve_leg(dml, torch, stream, c2_forest, c4_forests, c4_probs):
     ring = pinned(1 << 26)
     M = 6000
     rate = 100_000.0
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, M))
-    sizes = np.exp(rng.uniform(0.0, np.log(65536.0), M)).astype(np.int64)
-    which = rng.integers(0, len(forests), M)
-    reqs = []
-    for i in range(M):
-        fi = int(which[i])
-        F = infos[fi].n_features
-        n = int(sizes[i])
-        X = pools[forests[fi][1]][: F * n].reshape(F, n)
-        width = infos[fi].n_classes
-        off = (i * 997 * 64) % (ring.size - n * width)
-        reqs.append((fi, X, ring[off: off + n * width].reshape(n, width), n))
-    t0 = time.perf_counter()
-    ids = []
-    for i, (fi, X, out, n) in enumerate(reqs):
-        while time.perf_counter() - t0 < arrivals[i]:
-            pass
-        ids.append(srv.submit(fids[fi], X, out))
-    t_submit = time.perf_counter() - t0
-    lat = np.array([srv.wait(r) for r in ids])
+
+    def burst(seed):
+        """M requests with Poisson arrivals at `rate`; per-request latency
+        (submit to completion, measured by the server) and the burst's rows/s
+        from the first submit to the last completion."""
+        r = np.random.default_rng(seed)
+        arrivals = np.cumsum(r.exponential(1.0 / rate, M))
+        sizes = np.exp(r.uniform(0.0, np.log(65536.0), M)).astype(np.int64)
+        which = r.integers(0, len(forests), M)
+        reqs = []
+        for i in range(M):
+            fi = int(which[i])
+            F = infos[fi].n_features
+            n = int(sizes[i])
+            X = pools[forests[fi][1]][: F * n].reshape(F, n)
+            width = infos[fi].n_classes
+            off = (i * 997 * 64) % (ring.size - n * width)
+            reqs.append((fi, X, ring[off: off + n * width].reshape(n, width), n))
+        t0 = time.perf_counter()
+        ids, sub_t = [], []
+        for i, (fi, X, out, n) in enumerate(reqs):
+            while time.perf_counter() - t0 < arrivals[i]:
+                pass
+            sub_t.append(time.perf_counter() - t0)
+            ids.append(srv.submit(fids[fi], X, out))
+        t_submit = time.perf_counter() - t0
+        lat = np.array([srv.wait(q) for q in ids])
+        done = np.array(sub_t) + lat / 1000.0
+        rows = np.array([q[3] for q in reqs])
+        small = rows <= 4096
+        return reqs, {
+            "requests": M, "offered_req_per_s": M / t_submit,
+            "offered_rows_per_s": float(rows.sum()) / t_submit,
+            "rows_per_s": float(rows.sum()) / float(done.max() - sub_t[0]),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "le4k_requests": int(small.sum()),
+            "p50_ms_le4k": float(np.percentile(lat[small], 50)),
+            "p99_ms_le4k": float(np.percentile(lat[small], 99))}
+    bursts = []
+    for rep in range(3):
+        reqs, b = burst(5 + rep)
+        bursts.append(b)
     st = srv.stats()
-    small = np.array([r[3] <= 4096 for r in reqs])
     srv.close()
     # the plain path: each request alone through the reference's predict
     # structure (dml_predict_plain), one after another, on a sample of the stream
@@ -294,13 +397,19 @@ def serve_leg(dml, torch, stream, c2_forest, c4_forests, c4_probs):
     plain_rows_per_s = rows / (time.perf_counter() - tp)
     f1.free()
     f3.free()
-    return {"requests": M, "offered_req_per_s": M / t_submit, "rows_per_s": st.rows_per_s,
-            "small_rows": 4096, "plain": "dml_predict_plain on the first 600 requests",
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "p50_ms_le4k": float(np.percentile(lat[small], 50)),
-            "p99_ms_le4k": float(np.percentile(lat[small], 99)),
+    served = float(np.median([b["rows_per_s"] for b in bursts]))
+    return {"bursts": bursts, "requests_per_burst": M,
+            "offered": "Poisson arrivals at %.0f req/s, rows log-uniform in [1, 65536] "
+                       "(about %.0f M rows/s offered, above what the server completes, so "
+                       "the large-request queue grows during a burst)" % (
+                           rate, np.mean([b["offered_rows_per_s"] for b in bursts]) / 1e6),
+            "rows_per_s": served, "small_rows": 4096,
+            "p50_ms_le4k": float(np.median([b["p50_ms_le4k"] for b in bursts])),
+            "p99_ms_le4k_max": float(max(b["p99_ms_le4k"] for b in bursts)),
+            "server": "one server, three bursts of %d requests, idle between bursts" % M,
+            "plain": "dml_predict_plain on the first 600 requests of the last burst",
             "launches": st.launches, "plain_rows_per_s": plain_rows_per_s,
-            "speedup_vs_plain": st.rows_per_s / plain_rows_per_s}, configs
+            "speedup_vs_plain": served / plain_rows_per_s}, configs
 
 
 def run_ours(args, w):
@@ -388,6 +497,28 @@ def run_ours(args, w):
     torch.cuda.synchronize()
     predict_rows_per_s = 3 * w["rows"] / (pe0.elapsed_time(pe1) / 1000.0)
     finfo = last_forest.info()
+    predict_roofline = None
+    if rank == 0:
+        from datamininglibs_gb300 import model
+        pn, pp = last_forest.export()
+        path = model.mean_path_nodes(pn, pp, w["trees"], w["classes"])
+        del pn, pp
+        io_b = 4 * w["features"] + 4 * w["classes"]
+        node_b = 16 * w["trees"] * path
+        peak, peak_kind = measured_peak()
+        predict_roofline = {
+            "bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
+            "rows_per_s": predict_rows_per_s,
+            "io_bytes_per_row": io_b,
+            "mean_nodes_per_tree": path,
+            "node_bytes_per_row": node_b,
+            "achieved_io": predict_rows_per_s * io_b / 1e9,
+            "frac_io": predict_rows_per_s * io_b / 1e9 / peak,
+            "achieved_with_nodes": predict_rows_per_s * (io_b + node_b) / 1e9,
+            "frac_with_nodes": predict_rows_per_s * (io_b + node_b) / 1e9 / peak,
+            "note": "io = 4F + 4C bytes per row (row read once, votes written once); nodes = "
+                    "trees x mean nodes per walk x 16-byte predict nodes (loads, many from L2: "
+                    "the forest is %.0f MB)" % (finfo.n_nodes * 16 / 1e6)}
 
     # e2e: the C ABI with pinned host buffers, upload and model download timed.
     # The model is read into pinned buffers allocated once, as a caller that
@@ -426,6 +557,10 @@ def run_ours(args, w):
                                                              c4f, c4p)
         for f in c4f:
             f.free()
+    keep_model = world == 1 and not args.no_cpu
+    if keep_model:
+        timed_nodes, timed_probs = last_forest.export()
+        timed_gains = last_forest.gains()
     last_forest.free()
     if rank != 0:
         if dist is not None:
@@ -460,6 +595,7 @@ def run_ours(args, w):
         "trees_per_s": world * args.steps * w["trees"] / (dev_ms / 1000.0),
         "nodes_per_fit": nodes / args.steps,
         "predict_rows_per_s": predict_rows_per_s,
+        "predict_roofline": predict_roofline,
         "forest": {"nodes": finfo.n_nodes, "max_depth": finfo.max_depth},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
@@ -479,12 +615,48 @@ def run_ours(args, w):
         "clocks": clocks,
     }
     line.update(extras)
-    if world == 1 and not args.no_cpu:
+    if keep_model:
         th = os.cpu_count() or 1
-        line["cpu_baseline"] = cpu_baseline(w, X, y, th, th)
+        line["cpu_baseline"], m = cpu_baseline(w, X, y, th, min(th, w["trees"]), with_model=True)
+        line["parity"] = parity_of_timed_forest(w, timed_nodes, timed_probs, timed_gains, m)
+        del timed_nodes, timed_probs, timed_gains, m
+        if "other_configs" in line:
+            line["other_configs"]["cpu_baselines"] = other_cpu_baselines(th)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_predict_file(args, w):
+    """--save-forest: fit the workload's forest once and save it.  --predict-from:
+    load a saved forest and predict the workload's rows (resident on the
+    device) 3 times after one warm-up; prints rows/s.  The predict process then
+    holds only the forest, the rows and the votes (a few GB), the size an ncu
+    capture of the predict kernel wants."""
+    import torch
+
+    import datamininglibs_gb300 as dml
+    dml.lib()
+    X, y = make_data(w)
+    if args.save_forest:
+        f = dml.fit(X, y, **fit_kwargs(w))
+        f.save(args.save_forest)
+        print(json.dumps({"saved": args.save_forest, "nodes": f.info().n_nodes}), flush=True)
+        return
+    f = dml.Forest.load(args.predict_from)
+    Xd = torch.from_numpy(X).cuda()
+    out = torch.empty((w["rows"], w["classes"]), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    f.predict(Xd, out=out, stream=stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(3):
+        f.predict(Xd, out=out, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    print(json.dumps({"predict_rows_per_s": 3 * w["rows"] / (e0.elapsed_time(e1) / 1000.0),
+                      "nodes": f.info().n_nodes}), flush=True)
 
 
 def main():
@@ -499,9 +671,15 @@ def main():
                     help="skip the autotuner (default scheduling; for ncu launch indices)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the plain-path, batched-forest and serving legs")
+    ap.add_argument("--save-forest", default=None,
+                    help="fit the workload's forest once, save it to this file, exit")
+    ap.add_argument("--predict-from", default=None,
+                    help="load a saved forest and time predict on the workload's rows, exit")
     args = ap.parse_args()
     w = SMALL if args.small else WORKLOAD
-    if args.impl == "reference":
+    if args.save_forest or args.predict_from:
+        run_predict_file(args, w)
+    elif args.impl == "reference":
         run_reference(args, w)
     else:
         run_ours(args, w)

@@ -50,7 +50,7 @@ def build(verbose=False, extra=()):
             if err:
                 sys.stderr.write(err)
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lcudart", "-lpthread"]
+    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lcudart", "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

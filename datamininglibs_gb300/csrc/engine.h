@@ -80,4 +80,12 @@ Tuning tuning_for(const dml_fit_desc* descs, int nprob, int class_width);
 void* dev_alloc(size_t bytes, cudaStream_t s);
 void dev_free(void* p, cudaStream_t s);
 
+// Forced allocation failure, for failure-detection tests (host side only, no
+// device fault): with DML_FAIL_ALLOC=k in the environment, the k-th device
+// allocation made by one call of an entry point on the calling thread fails as
+// out of memory.  alloc_fault_arm() starts the count (each entry point calls
+// it); alloc_fault_fire() is true for the allocation that must fail.
+void alloc_fault_arm();
+bool alloc_fault_fire();
+
 }  // namespace dml

@@ -15,6 +15,8 @@
 #include <mutex>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "engine.h"
 #include "level_kernels.cuh"
 #include "search_launch.cuh"
@@ -85,8 +87,26 @@ int quant_scale_from_max(float mx, long long n) {
   return S;
 }
 
+namespace {
+thread_local long long t_alloc_count = 0;
+thread_local long long t_alloc_fail_at = 0;
+}  // namespace
+
+void alloc_fault_arm() {
+  t_alloc_count = 0;
+  const char* e = getenv("DML_FAIL_ALLOC");
+  t_alloc_fail_at = e ? std::atoll(e) : 0;
+}
+
+bool alloc_fault_fire() { return t_alloc_fail_at > 0 && ++t_alloc_count == t_alloc_fail_at; }
+
 void* dev_alloc(size_t bytes, cudaStream_t s) {
   if (bytes == 0) bytes = 16;
+  if (alloc_fault_fire()) {
+    set_error("device allocation of %zu bytes failed: out of memory (injected by DML_FAIL_ALLOC)",
+              bytes);
+    throw CudaError{cudaErrorMemoryAllocation};
+  }
   void* p = nullptr;
   cudaError_t e = cudaMallocAsync(&p, bytes, s);
   if (e != cudaSuccess) {
@@ -220,8 +240,27 @@ static void finish_stats(dml_fit_stats& st) { g_last_stats = st; }
 bool compute_ranks(const float* X, long long N, int F, uint32_t* rank, float* vals,
                    cudaStream_t s);
 
+// NVTX ranges (no-ops unless a profiler is attached): one per fit, one per
+// level, one per node class's launches.
+struct NvtxRange {
+  explicit NvtxRange(const char* fmt, ...) {
+    char buf[96];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    nvtxRangePushA(buf);
+  }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
+static const char* const kQueueNames[kNumQ] = {
+    "group32", "ert_cta", "rf_smem", "rf_big", "rf_warp64", "rf_warp128",
+    "rf_warp256", "group16", "group8", "rf_warp512", "ert_warp256"};
+
 static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bool plain,
                                         cudaStream_t s) {
+  NvtxRange fit_range("dml fit: %d forest(s)%s", nprob, plain ? ", plain" : "");
   init_pool_once();
   // ------------------------------------------------------------ checks
   std::vector<ProbDesc> hp(nprob);
@@ -569,6 +608,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     const char* tenv = getenv("DML_TRACE");
     const bool trace = tenv && tenv[0] == '1';
     while (n > 0) {
+      NvtxRange level_range("dml level %d: %d nodes", depth, n);
       // ------------------------------------------- search + partition
       LevelArgs a;
       a.probs = d_probs;
@@ -591,6 +631,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       float qms[kNumQ] = {};
       for (int q = 0; q < kNumQ; ++q) {
         if (qc[q] <= 0) continue;
+        NvtxRange class_range("dml search %s: %d nodes", kQueueNames[q], qc[q]);
         if (q == kQRfBig) {
           // per-(node, try) items on a persistent grid with per-CTA scratch
           const int nb = qc[q];
@@ -803,7 +844,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
                      al(sizeof(float) * std::max<long long>(1, fleaves[i] * hp[i].C)) +
                      al(sizeof(PNode) * std::max<long long>(1, fnodes[i]));
     ForestBlock* block = new ForestBlock();
-    if (cudaMalloc(&block->base, block_bytes) != cudaSuccess) {
+    if (alloc_fault_fire() || cudaMalloc(&block->base, block_bytes) != cudaSuccess) {
       delete block;
       cudaGetLastError();
       set_error("device allocation of %lld bytes for the forests failed", block_bytes);
@@ -915,6 +956,7 @@ static dml_status fit_entry(const dml_fit_desc* descs, int n, dml_forest** out, 
     return DML_ERR_INVALID_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  alloc_fault_arm();
   try {
     std::vector<dml_forest*> fs = run_fit(descs, n, plain, s);
     for (int i = 0; i < n; ++i) out[i] = fs[i];

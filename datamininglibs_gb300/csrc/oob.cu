@@ -172,6 +172,7 @@ extern "C" dml_status dml_oob_estimate(const dml_forest* f, const dml_fit_desc* 
   }
   std::memset(out, 0, sizeof(*out));
   init_pool_once();
+  alloc_fault_arm();
   cudaStream_t s = (cudaStream_t)stream;
   const long long N = d.n_rows;
   const int C = f->task == DML_CLASSIFICATION ? f->n_classes : 1;

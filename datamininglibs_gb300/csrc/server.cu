@@ -478,6 +478,7 @@ dml_status dml_server_create(const dml_server_config* cfg, dml_server** out) {
     return DML_ERR_INVALID_ARG;
   }
   init_pool_once();
+  alloc_fault_arm();
   dml_server* s = new dml_server();
   s->cfg = *cfg;
   s->small_rows = cfg->small_rows > 0 ? cfg->small_rows : 4096;
@@ -500,13 +501,16 @@ dml_status dml_server_create(const dml_server_config* cfg, dml_server** out) {
     const long long lane_rows = sl.small ? std::max<long long>(s->small_rows * 16, 65536)
                                          : cfg->max_batch_rows;
     sl.tile_cap = (int)std::min<long long>(1 << 22, lane_rows / kSplitRows + 1024);
+    auto dmalloc = [](void* p, size_t bytes) {  // device buffers; injectable failure
+      return !alloc_fault_fire() && cudaMalloc((void**)p, bytes) == cudaSuccess;
+    };
     ok = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking,
                                       sl.small ? prio_high : prio_low) == cudaSuccess &&
          cudaMallocHost(&sl.h_in, sl.cap) == cudaSuccess &&
          cudaMallocHost(&sl.h_out, sl.cap) == cudaSuccess &&
          cudaMallocHost(&sl.h_tiles, sizeof(PredTile) * sl.tile_cap) == cudaSuccess &&
-         cudaMalloc(&sl.d_in, sl.cap) == cudaSuccess && cudaMalloc(&sl.d_out, sl.cap) == cudaSuccess &&
-         cudaMalloc(&sl.d_tiles, sizeof(PredTile) * sl.tile_cap) == cudaSuccess &&
+         dmalloc(&sl.d_in, sl.cap) && dmalloc(&sl.d_out, sl.cap) &&
+         dmalloc(&sl.d_tiles, sizeof(PredTile) * sl.tile_cap) &&
          cudaEventCreateWithFlags(&sl.batch.done, cudaEventDisableTiming) == cudaSuccess;
   }
   if (!ok) {

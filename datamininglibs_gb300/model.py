@@ -41,3 +41,32 @@ def tree_arrays(nodes, probs, n_classes, tree, gains=None):
     if gains is None:
         return sub, sub_probs
     return sub, sub_probs, np.asarray(gains)[idx]
+
+
+def node_depths(nodes, n_trees):
+    """Depth of every node of a forest (roots 0..n_trees-1 at depth 0)."""
+    nodes = np.asarray(nodes, np.int32)
+    depth = np.full(nodes.shape[0], -1, np.int32)
+    frontier = np.arange(n_trees, dtype=np.int64)
+    d = 0
+    while frontier.size:
+        depth[frontier] = d
+        nd = nodes[frontier]
+        ch = nd[nd[:, 1] > 0, 0].astype(np.int64)
+        frontier = np.stack([ch, ch + 1], axis=1).reshape(-1)
+        d += 1
+    return depth
+
+
+def mean_path_nodes(nodes, probs, n_trees, n_classes):
+    """Nodes a prediction walk loads per tree, averaged over the rows the
+    forest was fitted on: each leaf's depth + 1 weighted by the training
+    weight that reached it (its class counts' sum; a tree of a bootstrap fit
+    holds as many draws as rows, so the weights estimate the rows' share)."""
+    nodes = np.asarray(nodes, np.int32)
+    depth = node_depths(nodes, n_trees)
+    leaf = nodes[:, 1] == 0
+    C = max(1, int(n_classes))
+    ps = nodes[leaf, 2].astype(np.int64)
+    w = np.asarray(probs, np.float64)[(ps[:, None] + np.arange(C)[None, :])].sum(axis=1)
+    return float(((depth[leaf] + 1) * w).sum() / w.sum())

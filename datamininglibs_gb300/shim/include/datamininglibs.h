@@ -131,7 +131,15 @@ class MlModel {
   T& Get(const int id) {
     return GetData(id).get_value<T>();
   }
-  virtual bool Has(const int id) = 0;
+  // Addition (not in the reference): whether slot `id` holds a value.  Models
+  // of this library override it.  A model class written against the
+  // reference's interface (AddData / GetData only) keeps this default, which
+  // reads the reference's own slots (below kReferenceSlotEnd) through GetData
+  // and reports the slots past them as empty.
+  virtual bool Has(const int id) {
+    return id >= 0 && id < kReferenceSlotEnd && !GetData(id).empty();
+  }
+  static constexpr int kReferenceSlotEnd = 6;  // ModelsInterface::kGpuDteModelEndMarker
 
  private:
   virtual void AddData(const int id, sutil::any_type data) = 0;
@@ -167,8 +175,18 @@ class MlAlgorithmParams {
   const T& Get(const int param) {
     return GetParam(param).get_value<T>();
   }
-  virtual bool Has(const int param) = 0;
-  virtual sp<MlAlgorithmParams> Clone() = 0;
+  // Additions (not in the reference): whether `param` holds a value, and a
+  // copy of the pack.  Packs of this library override both.  A pack class
+  // written against the reference's interface (SetParam / GetParam only) keeps
+  // these defaults: Has reads the reference's own ids (below kReferenceParamEnd)
+  // through GetParam and reports the ids past them as unset, and Clone returns
+  // null, for which SplitParameterPack copies the reference's ids into packs of
+  // its own.
+  virtual bool Has(const int param) {
+    return param >= 0 && param < kReferenceParamEnd && !GetParam(param).empty();
+  }
+  virtual sp<MlAlgorithmParams> Clone() { return nullptr; }
+  static constexpr int kReferenceParamEnd = 8;  // EnsemblesInterface::kDteEndMarker
 
  private:
   virtual void SetParam(const int param, const sutil::any_type value) = 0;
@@ -198,6 +216,12 @@ class AlgorithmsInterface {
   static AlgorithmsInterface& GetInstance();
   enum AlgorithmType { kClassification = 0, kRegression };
   sp<MlAlgorithmParams> CreateAlgorithmParams(int size);
+  // algorithms_interface.h:16 / algorithms_interface.cc:18-26: wraps a
+  // single-device algorithm into the multi-device one (trees split over the
+  // visible GPUs, one host thread each; models and votes aggregated).  T is
+  // float or double.
+  template <typename T>
+  sp<MlAlgorithm<T>> CreateGpuAlgorithm(sp<MlAlgorithm<T>> algo);
 };
 }  // namespace lib_algorithms
 using AlgorithmsLib = lib_algorithms::AlgorithmsInterface;
@@ -243,6 +267,12 @@ class EnsemblesInterface {
 };
 }  // namespace lib_ensembles
 using EnsemblesLib = lib_ensembles::EnsemblesInterface;
+static_assert(lib_algorithms::MlAlgorithmParams::kReferenceParamEnd ==
+                  (int)lib_ensembles::EnsemblesInterface::kDteEndMarker,
+              "reference parameter ids end at kDteEndMarker");
+static_assert(lib_models::MlModel::kReferenceSlotEnd ==
+                  (int)lib_models::ModelsInterface::kGpuDteModelEndMarker,
+              "reference model slots end at kGpuDteModelEndMarker");
 
 namespace lib_parsing {
 template <typename T>

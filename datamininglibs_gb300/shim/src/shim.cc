@@ -21,7 +21,9 @@
 #include "datamininglibs.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <functional>
@@ -212,6 +214,94 @@ sp<MlAlgorithmParams> AlgorithmsInterface::CreateAlgorithmParams(int size) {
 }
 }  // namespace lib_algorithms
 
+namespace lib_algorithms {
+namespace {
+// GpuAlgorithm<T>: the trees of a fit, or of a predict, spread over the
+// visible GPUs with one host thread each (gpu_algorithm.cc:17-50).
+template <typename T>
+class GpuAlgorithm : public MlAlgorithm<T> {
+  using MlModel = lib_models::MlModel;
+  template <typename U>
+  using MlDataFrame = lib_data::MlDataFrame<U>;
+  template <typename U>
+  using MlResultData = lib_data::MlResultData<U>;
+
+ public:
+  explicit GpuAlgorithm(sp<MlAlgorithm<T>> dev) : dev_(std::move(dev)) {}
+
+  sp<MlModel> Fit(sp<MlDataFrame<T>> data, sp<MlAlgorithmParams> params) override {
+    int count = devices(params);
+    if (count <= 1) return dev_->Fit(data, params);
+    auto packs = SplitParameterPack(params, count);
+    col_array<sp<MlModel>> models(count);
+    run(count, [&](int i) {
+      packs[i]->Set(EnsemblesLib::kDevId, i);
+      models[i] = dev_->Fit(data, packs[i]);
+    });
+    return AggregateModels(models);
+  }
+
+  sp<MlResultData<T>> Predict(sp<MlDataFrame<T>> data, sp<MlModel> model,
+                              sp<MlAlgorithmParams> params) override {
+    int count = devices(params);
+    if (count <= 1) return dev_->Predict(data, model, params);
+    auto parts = SplitModel(model, count);
+    col_array<sp<MlResultData<T>>> results(count);
+    run(count, [&](int i) { results[i] = dev_->Predict(data, parts[i], params); });
+    return AggregateResults(results);
+  }
+
+  sp<MlModel> AggregateModels(col_array<sp<MlModel>> m) override { return dev_->AggregateModels(m); }
+  col_array<sp<MlModel>> SplitModel(sp<MlModel> m, const int parts) override {
+    return dev_->SplitModel(m, parts);
+  }
+  sp<MlResultData<T>> AggregateResults(col_array<sp<MlResultData<T>>> r) override {
+    return dev_->AggregateResults(r);
+  }
+  col_array<sp<MlAlgorithmParams>> SplitParameterPack(sp<MlAlgorithmParams> p, const int parts) override {
+    return dev_->SplitParameterPack(p, parts);
+  }
+
+ private:
+  static int devices(const sp<MlAlgorithmParams>& params) {
+    int n = 1;
+    if (dml_device_count(&n) != DML_OK) n = 1;
+    // an explicit kDevId keeps the work on that one device
+    if (params->Has(EnsemblesLib::kDevId) && params->Get<int>(EnsemblesLib::kDevId) > 0) return 1;
+    return std::max(1, n);
+  }
+  template <class Fn>
+  static void run(int count, Fn fn) {
+    std::vector<std::thread> th;
+    std::vector<std::exception_ptr> err(count);
+    for (int i = 0; i < count; ++i)
+      th.emplace_back([&, i] {
+        try {
+          if (dml_set_device(i) != DML_OK) throw_status(DML_ERR_CUDA, "device selection");
+          fn(i);
+        } catch (...) {
+          err[i] = std::current_exception();
+        }
+      });
+    for (auto& t : th) t.join();
+    for (auto& e : err)
+      if (e) std::rethrow_exception(e);
+  }
+  sp<MlAlgorithm<T>> dev_;
+};
+}  // namespace
+
+template <typename T>
+sp<MlAlgorithm<T>> AlgorithmsInterface::CreateGpuAlgorithm(sp<MlAlgorithm<T>> algo) {
+  if (!algo) CoreLib::GetInstance().ThrowException("CreateGpuAlgorithm: no algorithm");
+  return std::make_shared<GpuAlgorithm<T>>(std::move(algo));
+}
+template sp<MlAlgorithm<float>> AlgorithmsInterface::CreateGpuAlgorithm<float>(
+    sp<MlAlgorithm<float>>);
+template sp<MlAlgorithm<double>> AlgorithmsInterface::CreateGpuAlgorithm<double>(
+    sp<MlAlgorithm<double>>);
+}  // namespace lib_algorithms
+
 // -------------------------------------------------------------- ensembles
 namespace lib_ensembles {
 namespace {
@@ -233,6 +323,24 @@ struct DeviceForest {
 
 int get_int(const sp<MlAlgorithmParams>& p, int id, int dflt) {
   return p->Has(id) ? p->Get<int>(id) : dflt;
+}
+
+// A pack of this library holding every parameter of `src` that it has, each
+// read with the type the reference stores it as (ensembles_interface.cc:28-58):
+// the copy SplitParameterPack makes of a pack class that cannot clone itself.
+sp<MlAlgorithmParams> copy_reference_params(const sp<MlAlgorithmParams>& src) {
+  auto q = AlgorithmsLib::GetInstance().CreateAlgorithmParams(EnsemblesLib::kGb300EndMarker);
+  const int ints[] = {EnsemblesLib::kDevId,   EnsemblesLib::kNrTrees,    EnsemblesLib::kNrFeatures,
+                      EnsemblesLib::kMaxDepth, EnsemblesLib::kMinNodeSize, EnsemblesLib::kMinLeaf,
+                      EnsemblesLib::kSeed,    EnsemblesLib::kTreeOffset};
+  for (int id : ints)
+    if (src->Has(id)) q->Set(id, src->Get<int>(id));
+  if (src->Has(EnsemblesLib::kAlgoType))
+    q->Set(EnsemblesLib::kAlgoType,
+           src->Get<AlgorithmsLib::AlgorithmType>(EnsemblesLib::kAlgoType));
+  for (int id : {(int)EnsemblesLib::kEasyEnsemble, (int)EnsemblesLib::kBagging})
+    if (src->Has(id)) q->Set(id, src->Get<bool>(id));
+  return q;
 }
 
 // The device forest of a model: the fitted one, or one imported from the
@@ -290,6 +398,51 @@ void append_tree(const col_array<Node<T>>& nodes, const col_array<T>& probs, int
   }
 }
 
+// The engine fits and predicts in FP32 (its gains, thresholds and tie rules are
+// pinned for FP32).  A double frame (the reference's MlAlgorithm<double>,
+// gpudte.cu:391-420) is fitted only when every value is a float exactly:
+// then the sort order, the candidate boundaries and the partitions are the ones
+// the values define, and the fit equals the float frame's.  Any other value is
+// refused with an exception naming it, never narrowed silently.  Thresholds
+// are float midpoints, widened exactly into the model's double split points.
+template <typename T>
+std::vector<float> exact_floats(const col_array<T>& v, const char* what) {
+  std::vector<float> out(v.size());
+  for (size_t i = 0; i < v.size(); ++i) {
+    out[i] = (float)v[i];
+    if (!((T)out[i] == v[i]) && !(v[i] != v[i])) {
+      char buf[160];
+      std::snprintf(buf, sizeof(buf),
+                    "Fit: %s %zu (%.17g) is not exactly a float; this engine fits in FP32 and "
+                    "takes double frames whose values are floats", what, i, (double)v[i]);
+      CoreLib::GetInstance().ThrowException(buf);
+    }
+  }
+  return out;
+}
+
+// Predict values for the FP32 walk: each value rounded toward -infinity to a
+// float (values below -FLT_MAX become -FLT_MAX, which goes left like any value
+// below a threshold).  For a float threshold t, x < t exactly when the rounded
+// value is below t, so a double frame gets the votes the reference's double
+// comparison gives on this model's thresholds.
+template <typename T>
+std::vector<float> rounded_down(const col_array<T>& v) {
+  std::vector<float> out(v.size());
+  for (size_t i = 0; i < v.size(); ++i) {
+    const T x = v[i];
+    float f = (float)x;
+    if (x != x) {
+      out[i] = f;
+      continue;
+    }
+    if ((T)f > x) f = std::nextafter(f, -INFINITY);
+    if (f < -FLT_MAX) f = -FLT_MAX;
+    out[i] = f;
+  }
+  return out;
+}
+
 // Fit / Predict of one device (GpuDteAlgorithm<T>).
 template <typename T>
 class DteAlgorithm : public MlAlgorithm<T> {
@@ -304,8 +457,8 @@ class DteAlgorithm : public MlAlgorithm<T> {
     const int C = type == AlgorithmsLib::kClassification ? data->GetNrTargets() : 1;
     if ((long long)N * F != (long long)data->GetSamples().size())
       CoreLib::GetInstance().ThrowException("data frame: samples do not hold features x rows values");
-    std::vector<float> xs(data->GetSamples().begin(), data->GetSamples().end());
-    std::vector<float> ys(data->GetTargets().begin(), data->GetTargets().end());
+    std::vector<float> xs = exact_floats(data->GetSamples(), "sample");
+    std::vector<float> ys = exact_floats(data->GetTargets(), "target");
     dml_fit_desc d;
     std::memset(&d, 0, sizeof(d));
     d.algo = algo_;
@@ -366,7 +519,7 @@ class DteAlgorithm : public MlAlgorithm<T> {
     dml_forest_info info;
     dml_forest_info_get(f, &info);
     const int width = info.task == DML_CLASSIFICATION ? info.n_classes : 1;
-    std::vector<float> xs(data->GetSamples().begin(), data->GetSamples().end());
+    std::vector<float> xs = rounded_down(data->GetSamples());
     if ((long long)xs.size() != (long long)N * info.n_features)
       CoreLib::GetInstance().ThrowException("Predict: the frame's feature count differs from the model's");
     std::vector<float> out((size_t)N * width);
@@ -452,6 +605,7 @@ class DteAlgorithm : public MlAlgorithm<T> {
     for (int p = 0; p < parts; ++p) {
       const int k = trees / parts + (p < trees % parts ? 1 : 0);
       auto q = params->Clone();
+      if (!q) q = copy_reference_params(params);
       q->Set(EnsemblesLib::kNrTrees, k);
       q->Set(EnsemblesLib::kTreeOffset, off0 + t0);
       out.push_back(q);
@@ -464,73 +618,6 @@ class DteAlgorithm : public MlAlgorithm<T> {
   int algo_;
 };
 
-// GpuAlgorithm<T>: the trees of a fit, or of a predict, spread over the
-// visible GPUs with one host thread each (gpu_algorithm.cc:17-50).
-template <typename T>
-class GpuAlgorithm : public MlAlgorithm<T> {
- public:
-  explicit GpuAlgorithm(sp<MlAlgorithm<T>> dev) : dev_(std::move(dev)) {}
-
-  sp<MlModel> Fit(sp<MlDataFrame<T>> data, sp<MlAlgorithmParams> params) override {
-    int count = devices(params);
-    if (count <= 1) return dev_->Fit(data, params);
-    auto packs = SplitParameterPack(params, count);
-    col_array<sp<MlModel>> models(count);
-    run(count, [&](int i) {
-      packs[i]->Set(EnsemblesLib::kDevId, i);
-      models[i] = dev_->Fit(data, packs[i]);
-    });
-    return AggregateModels(models);
-  }
-
-  sp<MlResultData<T>> Predict(sp<MlDataFrame<T>> data, sp<MlModel> model,
-                              sp<MlAlgorithmParams> params) override {
-    int count = devices(params);
-    if (count <= 1) return dev_->Predict(data, model, params);
-    auto parts = SplitModel(model, count);
-    col_array<sp<MlResultData<T>>> results(count);
-    run(count, [&](int i) { results[i] = dev_->Predict(data, parts[i], params); });
-    return AggregateResults(results);
-  }
-
-  sp<MlModel> AggregateModels(col_array<sp<MlModel>> m) override { return dev_->AggregateModels(m); }
-  col_array<sp<MlModel>> SplitModel(sp<MlModel> m, const int parts) override {
-    return dev_->SplitModel(m, parts);
-  }
-  sp<MlResultData<T>> AggregateResults(col_array<sp<MlResultData<T>>> r) override {
-    return dev_->AggregateResults(r);
-  }
-  col_array<sp<MlAlgorithmParams>> SplitParameterPack(sp<MlAlgorithmParams> p, const int parts) override {
-    return dev_->SplitParameterPack(p, parts);
-  }
-
- private:
-  static int devices(const sp<MlAlgorithmParams>& params) {
-    int n = 1;
-    if (dml_device_count(&n) != DML_OK) n = 1;
-    // an explicit kDevId keeps the work on that one device
-    if (params->Has(EnsemblesLib::kDevId) && params->Get<int>(EnsemblesLib::kDevId) > 0) return 1;
-    return std::max(1, n);
-  }
-  template <class Fn>
-  static void run(int count, Fn fn) {
-    std::vector<std::thread> th;
-    std::vector<std::exception_ptr> err(count);
-    for (int i = 0; i < count; ++i)
-      th.emplace_back([&, i] {
-        try {
-          if (dml_set_device(i) != DML_OK) throw_status(DML_ERR_CUDA, "device selection");
-          fn(i);
-        } catch (...) {
-          err[i] = std::current_exception();
-        }
-      });
-    for (auto& t : th) t.join();
-    for (auto& e : err)
-      if (e) std::rethrow_exception(e);
-  }
-  sp<MlAlgorithm<T>> dev_;
-};
 }  // namespace
 
 EnsemblesInterface& EnsemblesInterface::GetInstance() {
@@ -540,11 +627,13 @@ EnsemblesInterface& EnsemblesInterface::GetInstance() {
 
 template <typename T>
 sp<lib_algorithms::MlAlgorithm<T>> EnsemblesInterface::CreateGpuRfAlgorithm() {
-  return std::make_shared<GpuAlgorithm<T>>(std::make_shared<DteAlgorithm<T>>(DML_ALGO_RF));
+  return AlgorithmsLib::GetInstance().CreateGpuAlgorithm<T>(
+      std::make_shared<DteAlgorithm<T>>(DML_ALGO_RF));
 }
 template <typename T>
 sp<lib_algorithms::MlAlgorithm<T>> EnsemblesInterface::CreateGpuErtAlgorithm() {
-  return std::make_shared<GpuAlgorithm<T>>(std::make_shared<DteAlgorithm<T>>(DML_ALGO_ERT));
+  return AlgorithmsLib::GetInstance().CreateGpuAlgorithm<T>(
+      std::make_shared<DteAlgorithm<T>>(DML_ALGO_ERT));
 }
 
 static sp<lib_algorithms::MlAlgorithmParams> default_pack(bool bagging) {

@@ -214,7 +214,7 @@ int main(int argc, char** argv) {
   std::vector<sp<lib_data::MlResultData<float>>> rs;
   for (auto& m : split) rs.push_back(rf->Predict(df, m, params));
   CHECK(votes(rf->AggregateResults(rs)) == votes(res));
-  // double frames give the same forest (values are narrowed to float)
+  // double frames whose values are floats give the same forest
   auto dfd = DataLib::GetInstance().CreateDataFrame<double>();
   dfd->AddSampleData(std::vector<double>(X.begin(), X.end()));
   dfd->AddTargetData(std::vector<double>(y.begin(), y.end()));

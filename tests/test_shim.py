@@ -100,3 +100,42 @@ def test_shim_fit_predict_split_aggregate(shim_test, tmp_path):
     m = oracle.fit(X, y, algo=1, n_trees=100, K=0, max_depth=1000, min_node_size=5,
                    n_classes=4, seed=0)
     assert np.array_equal(nodes, m.nodes) and np.array_equal(probs, m.probs)
+
+
+@pytest.fixture(scope="session")
+def reference_style_test(tmp_path_factory, shim_test):
+    exe = str(tmp_path_factory.mktemp("refstyle") / "reference_style_test")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I" + os.path.join(PKG, "shim", "include"),
+                    os.path.join(HERE, "cpp", "reference_style_test.cc"), "-o", exe, "-L" + PKG,
+                    "-ldml_gb300_shim", "-ldml_gb300", "-Wl,-rpath," + PKG], check=True)
+    return exe
+
+
+def test_reference_style_classes_on_the_host(reference_style_test):
+    """A pack class and a model class written as the reference writes them
+    (SetParam / GetParam, AddData / GetData only) compile against the drop-in;
+    SplitParameterPack through AlgorithmsInterface::CreateGpuAlgorithm copies
+    such a pack (no GPU)."""
+    r = subprocess.run([reference_style_test, "host"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "host ok" in r.stdout
+
+
+@pytest.mark.gpu
+def test_reference_style_program_fits(reference_style_test, tmp_path):
+    """The ensembles_interface.cc:14-26 pattern (a single-device algorithm
+    wrapped by CreateGpuAlgorithm<T>) fitted with a reference-style pack gives
+    the library factory's forest; a reference-style model predicts alike; a
+    double frame of float values gives the float forest, one with a value no
+    float equals is refused, and double predictions equal a double walk of the
+    model on the host."""
+    from datamininglibs_gb300 import synth
+    X, y = synth.rf_multiclass(2000, 10, n_classes=3, n_int=2, seed=12)
+    with open(tmp_path / "data.bin", "wb") as f:
+        f.write(np.array([X.shape[1], X.shape[0], 3], np.int32).tobytes())
+        f.write(X.tobytes())
+        f.write(y.tobytes())
+    r = subprocess.run([reference_style_test, "fit", str(tmp_path / "data.bin")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "reference style ok" in r.stdout
