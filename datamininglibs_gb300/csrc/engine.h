@@ -87,5 +87,8 @@ void dev_free(void* p, cudaStream_t s);
 // it); alloc_fault_fire() is true for the allocation that must fail.
 void alloc_fault_arm();
 bool alloc_fault_fire();
+// ": out of memory (injected by DML_FAIL_ALLOC)" once this call's injected
+// failure has fired, else "" (appended to allocation error messages).
+const char* alloc_fault_note();
 
 }  // namespace dml

@@ -100,6 +100,12 @@ void alloc_fault_arm() {
 
 bool alloc_fault_fire() { return t_alloc_fail_at > 0 && ++t_alloc_count == t_alloc_fail_at; }
 
+const char* alloc_fault_note() {
+  return t_alloc_fail_at > 0 && t_alloc_count >= t_alloc_fail_at
+             ? ": out of memory (injected by DML_FAIL_ALLOC)"
+             : "";
+}
+
 void* dev_alloc(size_t bytes, cudaStream_t s) {
   if (bytes == 0) bytes = 16;
   if (alloc_fault_fire()) {
@@ -847,7 +853,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     if (alloc_fault_fire() || cudaMalloc(&block->base, block_bytes) != cudaSuccess) {
       delete block;
       cudaGetLastError();
-      set_error("device allocation of %lld bytes for the forests failed", block_bytes);
+      set_error("device allocation of %lld bytes for the forests failed%s", block_bytes,
+                alloc_fault_note());
       throw CudaError{cudaErrorMemoryAllocation};
     }
     char* bp = (char*)block->base;

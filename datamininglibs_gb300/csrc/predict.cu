@@ -10,6 +10,7 @@
 // deterministic.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -72,6 +73,35 @@ __global__ void __launch_bounds__(kPredBlock) k_predict(const PNode* __restrict_
   }
 }
 
+// Bulk predict in passes over blocks of trees.  A forest larger than L2 (the
+// 128-tree, 1M-row forest is 692 MB) walked by many row tiles at once touches
+// every tree's nodes at the same time, so almost every visit of a deep node is
+// a DRAM miss.  In passes, every CTA of a launch walks the same block of trees,
+// sized to sit well inside L2; node loads carry an L2 evict-last policy and
+// the streamed rows evict-first, so a pass's nodes come from DRAM about once.
+__device__ __forceinline__ unsigned long long l2_policy_evict_last() {
+  unsigned long long p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ unsigned long long l2_policy_evict_first() {
+  unsigned long long p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ int4 ld_node(const int4* p, unsigned long long pol) {
+  int4 v;
+  asm("ld.global.nc.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+      : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ld_stream(const float* p, unsigned long long pol) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+
 // Rows in tiles of 16, their features staged in shared memory (a row reads
 // one feature per node on its paths: from global memory those reads scatter
 // over the whole sample matrix), 8 threads per row walking trees g, g + 8, ...
@@ -86,33 +116,36 @@ constexpr int kPStride = kPRows + 1;
 
 template <int TASK>
 __global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __restrict__ nodes,
-                                                              int n_trees, int C, int F,
-                                                              const float* __restrict__ X,
+                                                              int t0, int t1, int first, int C,
+                                                              int F, const float* __restrict__ X,
                                                               long long N, float* __restrict__ out) {
-  extern __shared__ float psm[];  // xs [F][kPStride], then votes [kPRows][C] or values [kPRows][n_trees]
+  extern __shared__ float psm[];  // xs [F][kPStride], then votes [kPRows][C] or values [kPRows][t1 - t0]
   const long long row0 = (long long)blockIdx.x * kPRows;
   const int rows = N - row0 < kPRows ? (int)(N - row0) : kPRows;
   const int g = threadIdx.x % kPSplit;
   const int r = threadIdx.x / kPSplit;
+  const int nt = t1 - t0;
+  const unsigned long long keep = l2_policy_evict_last();
+  const unsigned long long stream = l2_policy_evict_first();
   float* xs = psm;
   for (int e = threadIdx.x; e < F * kPRows; e += kPredBlock) {
     const int f = e / kPRows, rr = e % kPRows;
-    xs[f * kPStride + rr] = rr < rows ? __ldg(X + (long long)f * N + row0 + rr) : 0.0f;
+    xs[f * kPStride + rr] = rr < rows ? ld_stream(X + (long long)f * N + row0 + rr, stream) : 0.0f;
   }
   int* votes = reinterpret_cast<int*>(psm + F * kPStride);
-  float* vals = psm + F * kPStride + r * n_trees;
+  float* vals = psm + F * kPStride + r * nt;
   if (TASK == 0)
     for (int i = threadIdx.x; i < kPRows * C; i += kPredBlock) votes[i] = 0;
   __syncthreads();
   if (r < rows) {
     const int4* nd = reinterpret_cast<const int4*>(nodes);
     // trees k, k + 8, k + 16, k + 24 in lockstep (four node loads in flight)
-    for (int k0 = g; k0 < n_trees; k0 += 4 * kPSplit) {
+    for (int k0 = t0 + g; k0 < t1; k0 += 4 * kPSplit) {
       int4 lf[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int k = k0 + j * kPSplit;
-        lf[j] = k < n_trees ? __ldg(nd + k) : make_int4(-1, 0, 0, 0);
+        lf[j] = k < t1 ? ld_node(nd + k, keep) : make_int4(-1, 0, 0, 0);
       }
       bool more = true;
       while (more) {
@@ -120,20 +153,21 @@ __global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __res
 #pragma unroll
         for (int j = 0; j < 4; ++j)
           if (lf[j].x >= 0) {
-            lf[j] = __ldg(nd + (goes_left(xs[lf[j].y * kPStride + r], __int_as_float(lf[j].z))
-                                    ? lf[j].x
-                                    : lf[j].x + 1));
+            lf[j] = ld_node(nd + (goes_left(xs[lf[j].y * kPStride + r], __int_as_float(lf[j].z))
+                                      ? lf[j].x
+                                      : lf[j].x + 1),
+                            keep);
             more = more || lf[j].x >= 0;
           }
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int k = k0 + j * kPSplit;
-        if (k < n_trees) {
+        if (k < t1) {
           if (TASK == 0)
             atomicAdd(&votes[r * C + lf[j].y], 1);
           else
-            vals[k] = __int_as_float(lf[j].z);
+            vals[k - t0] = __int_as_float(lf[j].z);
         }
       }
     }
@@ -142,13 +176,30 @@ __global__ void __launch_bounds__(kPredBlock) k_predict_split(const PNode* __res
   if (r < rows) {
     const long long row = row0 + r;
     if (TASK == 0) {
-      for (int c = g; c < C; c += kPSplit) out[row * C + c] = (float)votes[r * C + c];
+      for (int c = g; c < C; c += kPSplit) {
+        const float v = (float)votes[r * C + c];
+        out[row * C + c] = first ? v : __fadd_rn(out[row * C + c], v);
+      }
     } else if (g == 0) {
-      float sum = 0.0f;
-      for (int t = 0; t < n_trees; ++t) sum = __fadd_rn(sum, vals[t]);
+      // the pass's trees added one at a time in tree order onto the sum of
+      // the earlier passes: the same float additions as one pass
+      float sum = first ? 0.0f : out[row];
+      for (int t = 0; t < nt; ++t) sum = __fadd_rn(sum, vals[t]);
       out[row] = sum;
     }
   }
+}
+
+// Trees per pass: the pass's share of the predict nodes within kPassBytes.
+constexpr long long kPassBytes = 96ll << 20;
+int predict_pass_trees(const dml_forest* f) {
+  const char* e = getenv("DML_PREDICT_PASS_MB");
+  const long long budget = e && atoll(e) > 0 ? (atoll(e) << 20) : kPassBytes;
+  const long long per_tree = std::max<long long>(1, f->n_nodes * (long long)sizeof(PNode) /
+                                                        std::max(1, f->n_trees));
+  long long k = budget / per_tree;
+  k = std::max<long long>(kPSplit, (k / kPSplit) * kPSplit);
+  return (int)std::min<long long>(k, f->n_trees);
 }
 
 // The reference's predict structure (gpudte.cu:311-359): one thread per
@@ -173,25 +224,34 @@ __global__ void k_predict_plain(const PNode* __restrict__ nodes, int tree, int C
     out[row] = __fadd_rn(out[row], __int_as_float(p.z));
 }
 
+// Rows predicted in passes over blocks of trees from this many rows on (below
+// it, one pass over every tree).
+constexpr long long kPassMinRows = 1 << 16;
+
 dml_status predict_device(const dml_forest* f, const float* dX, long long n_rows, float* dout,
                           cudaStream_t s) {
   if (n_rows <= 0) return DML_OK;
+  const bool cls = f->task == DML_CLASSIFICATION;
+  const int per = n_rows >= kPassMinRows ? predict_pass_trees(f) : f->n_trees;
   // staged rows when the tile (features, votes or per-tree values) fits 48 KB
   const size_t split_sm =
       sizeof(float) * ((size_t)kPStride * f->n_features +
-                       (size_t)kPRows * (f->task == DML_CLASSIFICATION ? f->n_classes : f->n_trees));
+                       (size_t)kPRows * (cls ? f->n_classes : std::min(per, f->n_trees)));
   if (split_sm <= 48 * 1024) {
     const long long tiles = (n_rows + kPRows - 1) / kPRows;
-    if (f->task == DML_CLASSIFICATION)
-      k_predict_split<0><<<(unsigned)tiles, kPredBlock, split_sm, s>>>(
-          f->pnodes, f->n_trees, f->n_classes, f->n_features, dX, n_rows, dout);
-    else
-      k_predict_split<1><<<(unsigned)tiles, kPredBlock, split_sm, s>>>(
-          f->pnodes, f->n_trees, 1, f->n_features, dX, n_rows, dout);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-      set_error("predict launch failed: %s", cudaGetErrorString(e));
-      return DML_ERR_CUDA;
+    for (int t0 = 0; t0 < f->n_trees; t0 += per) {
+      const int t1 = std::min(f->n_trees, t0 + per);
+      if (cls)
+        k_predict_split<0><<<(unsigned)tiles, kPredBlock, split_sm, s>>>(
+            f->pnodes, t0, t1, t0 == 0, f->n_classes, f->n_features, dX, n_rows, dout);
+      else
+        k_predict_split<1><<<(unsigned)tiles, kPredBlock, split_sm, s>>>(
+            f->pnodes, t0, t1, t0 == 0, 1, f->n_features, dX, n_rows, dout);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) {
+        set_error("predict launch failed: %s", cudaGetErrorString(e));
+        return DML_ERR_CUDA;
+      }
     }
     return DML_OK;
   }

@@ -515,7 +515,8 @@ dml_status dml_server_create(const dml_server_config* cfg, dml_server** out) {
   }
   if (!ok) {
     cudaGetLastError();
-    set_error("could not allocate the server's streams and staging buffers");
+    set_error("could not allocate the server's streams and staging buffers%s",
+              alloc_fault_note());
     s->stop = true;
     dml_server_destroy(s);
     return DML_ERR_OOM;

@@ -25,8 +25,10 @@ def dml():
 
 
 def _sweep(monkeypatch, call, check, max_k=400):
-    """Runs call() with DML_FAIL_ALLOC = 1, 2, ... until five calls in a row
-    complete (k past the call's allocations); returns the number of OOMs."""
+    """Runs call() with DML_FAIL_ALLOC = 1, 2, ... until thirty calls in a row
+    complete (k past the call's allocations: the value ranks' temporaries fall
+    back rather than fail, so a few completions can come between failures);
+    returns the number of OOMs."""
     ooms, streak = 0, 0
     for k in range(1, max_k):
         monkeypatch.setenv("DML_FAIL_ALLOC", str(k))
@@ -42,7 +44,7 @@ def _sweep(monkeypatch, call, check, max_k=400):
             monkeypatch.delenv("DML_FAIL_ALLOC", raising=False)
         check(out)
         streak += 1
-        if streak >= 5:
+        if streak >= 30:
             break
     return ooms
 
@@ -59,7 +61,7 @@ def test_fit_survives_a_failure_at_every_allocation(dml, monkeypatch):
         assert np.array_equal(nodes, m.nodes) and np.array_equal(probs, m.probs)
 
     ooms = _sweep(monkeypatch, lambda: dml.fit(X, y, **kw), check)
-    assert ooms >= 20
+    assert ooms >= 15
     check(dml.fit(X, y, **kw))
 
 
@@ -82,7 +84,7 @@ def test_batched_fit_and_regression_survive_failures(dml, monkeypatch):
             f.free()
             assert np.array_equal(nodes, m.nodes) and np.array_equal(pr, m.probs)
 
-    assert _sweep(monkeypatch, lambda: dml.fit_batched(specs), check) >= 20
+    assert _sweep(monkeypatch, lambda: dml.fit_batched(specs), check) >= 15
 
 
 def test_oob_estimate_survives_failures(dml, monkeypatch):

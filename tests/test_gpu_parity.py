@@ -450,3 +450,25 @@ def test_forest_file_roundtrip(dml, tmp_path):
     open(bad, "wb").write(bytes(raw))
     with pytest.raises(dml.DmlError):
         dml.Forest.load(bad)
+
+
+@pytest.mark.parametrize("task", [0, 1])
+@pytest.mark.parametrize("pass_mb", [None, "1"])
+def test_bulk_predict_in_tree_passes_matches_oracle(dml, monkeypatch, task, pass_mb):
+    """Predictions of 70,000 rows (the bulk path: passes over blocks of trees,
+    votes and regression sums carried between passes) equal the oracle's, bit
+    for bit; DML_PREDICT_PASS_MB=1 forces a pass per few trees."""
+    if pass_mb:
+        monkeypatch.setenv("DML_PREDICT_PASS_MB", pass_mb)
+    if task == 0:
+        X, y = synth.rf_multiclass(70000, 24, n_classes=7, n_int=4, seed=41)
+        kw = dict(algo=0, n_trees=40, K=5, max_depth=14, min_node_size=5, n_classes=7, seed=5)
+    else:
+        X, y = synth.rf_regression(70000, 12, seed=42)
+        kw = dict(algo=0, task=1, n_trees=37, K=4, max_depth=12, min_node_size=5, min_leaf=3,
+                  seed=6)
+    m = oracle.fit(X, y, **kw)
+    f = dml.fit(X, y, **kw)
+    nodes, probs = f.export()
+    _assert_same_model(m, nodes, probs)
+    assert np.array_equal(f.predict(X), oracle.predict(m, X))
