@@ -30,8 +30,9 @@ struct BigSmem {
   unsigned tstart[256];
   unsigned running[2][256];
   unsigned red[2 * kBigWarps];
-  uint32_t tk[kBigTile];
-  uint32_t tv[kBigTile];
+  // a pass's tile: keys in [0, kBigTile), values after them; the class
+  // columns of the classification scan once the sort is done
+  uint32_t tile[2 * kBigTile];
   unsigned long long scan64[kBigWarps * (kMaxClasses / 2 + 1)];  // block_excl_scan_n, CW + 1 values
   unsigned scan32[kBigWarps];
   unsigned dh[4][256];  // per-digit histograms of the item's keys, counted while gathering
@@ -77,8 +78,9 @@ static __device__ __forceinline__ unsigned digit_excl_scan(unsigned tot, unsigne
 }
 
 // One LSD pass of pairs (kin, vin) -> (kout, vout) on byte `shift`, whose
-// digit histogram over all m keys is dh.  Scratch written earlier in the same
-// kernel is read with plain loads (never the read-only cache path).
+// digit histogram over all m keys is dh; a null vin stands for the values
+// 0 .. m-1.  Scratch written earlier in the same kernel is read with plain
+// loads (never the read-only cache path).
 static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                                 uint32_t* vout, int m, int shift, const unsigned* dh,
                                 BigSmem& S) {
@@ -101,7 +103,7 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
     for (int r = 0; r < kBigPer; ++r) {
       const int i = wbeg + r * 32 + lane;
       k[r] = i < tn ? kin[base + i] : 0u;
-      v[r] = i < tn ? vin[base + i] : 0u;
+      v[r] = i < tn ? (vin ? vin[base + i] : (uint32_t)(base + i)) : 0u;
     }
     for (int i = lane; i < 256; i += 32) S.whist[warp][i] = 0;
     __syncwarp();
@@ -149,8 +151,8 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
         const unsigned dgt = (k[r] >> shift) & 255u;
         const unsigned peers = pr[r];
         const unsigned pos = S.whist[warp][dgt] + __popc(peers & lt);
-        S.tk[pos] = k[r];
-        S.tv[pos] = v[r];
+        S.tile[pos] = k[r];
+        S.tile[kBigTile + pos] = v[r];
         __syncwarp(mask);
         if ((peers & lt) == 0) S.whist[warp][dgt] += __popc(peers);
       }
@@ -158,31 +160,34 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
     }
     __syncthreads();
     for (int j = threadIdx.x; j < tn; j += kBigBlock) {
-      const uint32_t kk = S.tk[j];
+      const uint32_t kk = S.tile[j];
       const unsigned dgt = (kk >> shift) & 255u;
       const unsigned pos = S.running[cur][dgt] + (j - S.tstart[dgt]);
       kout[pos] = kk;
-      vout[pos] = S.tv[j];
+      vout[pos] = S.tile[kBigTile + j];
     }
     __syncthreads();
     cur ^= 1;
   }
 }
 
-// Sorts (k, v) of length m whose varying key bits are `diff` and whose digit
-// histograms are S.dh.  Passes whose byte is the same in every key are
+// Sorts the keys k of length m, whose varying bits are `diff` (not 0) and
+// whose digit histograms are S.dh, with their values: the first pass reads
+// the values from v0 (null: 0 .. m-1), later passes from the buffer the
+// previous pass wrote.  Passes whose byte is the same in every key are
 // skipped; returns true when the result is in (k2, v2), false when in (k, v).
-static __device__ bool big_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2, int m,
-                                unsigned diff, BigSmem& S) {
-  bool primary = true;
+static __device__ bool big_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t* v2,
+                                const uint32_t* v0, int m, unsigned diff, BigSmem& S) {
+  bool primary = true, first = true;
   for (int d = 0; d < 4; ++d) {
     const int shift = 8 * d;
     if (((diff >> shift) & 255u) == 0) continue;
     if (primary)
-      big_pass(k, v, k2, v2, m, shift, S.dh[d], S);
+      big_pass(k, first ? v0 : v, k2, v2, m, shift, S.dh[d], S);
     else
       big_pass(k2, v2, k, v, m, shift, S.dh[d], S);
     primary = !primary;
+    first = false;
     __syncthreads();
   }
   return !primary;
@@ -207,6 +212,7 @@ struct BigArgs {
   int* big_index;          // node id -> index in `big` (for phase 2)
   uint32_t* pv;            // classification: label << 27 | weight per entry slot of the big nodes
   long long* pq;           // regression: packed (target, weight) per entry slot of the big nodes
+  int* item_ctr;           // [phase - 1]: items handed out so far, zero before the launch
 };
 
 // Per-entry values of the big nodes, once per level instead of a gather by
@@ -413,6 +419,142 @@ static __device__ __noinline__ void big_boundary_items(const uint32_t* sk, const
                          outL);
 }
 
+// Per-thread class counts of the column scan below: column c of thread t at
+// c * kColStride + t + t / 32 (one pad word per 32 threads, so that a lane
+// reading eight consecutive threads' words and a thread reading its own word
+// both meet 32 different banks).
+constexpr int kColStride = kBigBlock + kBigBlock / 32;
+__device__ __forceinline__ int col_of(int t) { return t + (t >> 5); }
+
+// Classification boundary scan with the class counts in shared memory:
+// column c < C holds each thread's count of class c, column C its row count.
+// Per tile of 256 * per sorted elements (per = 1..8 consecutive elements a
+// thread) each thread adds its elements' weights to its own words; one warp per column turns the words into exclusive prefixes
+// (eight words a lane, a warp scan of the lane totals, the column's carry from
+// the earlier tiles); the incremental scan then reads and moves the one count
+// an element changes, where the register form selects among the packed words
+// for every class on every element.  Results equal big_boundary<CW, INCR>.
+// cols: (C + 1) * kColStride words and C + 1 carries after them; nt: the
+// node's class counts (shared memory).  Two CTA barriers per tile.
+template <int CW>
+static __device__ __noinline__ void big_boundary_cols(const uint32_t* sk, const uint32_t* sv,
+                                                      int m, int per, const LNode& nd, int C,
+                                                      int ml,
+                                                      const long long* H, long long prior,
+                                                      const int* nt, uint32_t* cols,
+                                                      float* out_g, int* out_p, long long* out_nl,
+                                                      unsigned long long (&outL)[CW]) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int me = col_of(tid);
+  uint32_t* carry = cols + (C + 1) * kColStride;
+  if (tid <= C) carry[tid] = 0;
+  NumBest nb;
+  nb.init();
+  long long bnl = 0;
+  unsigned long long bL[CW];
+#pragma unroll
+  for (int j = 0; j < CW; ++j) bL[j] = 0;
+  for (int base = 0; base < m; base += kBigBlock * per) {
+    const int p0 = base + tid * per;
+    const uint32_t prevk0 = p0 > 0 && p0 - 1 < m ? sk[p0 - 1] : 0u;
+    for (int c = 0; c <= C; ++c) cols[c * kColStride + me] = 0;
+    uint32_t vq[kBigPer];
+    unsigned bnd = 0;
+    uint32_t tn = 0;
+    {
+      uint32_t prev = prevk0;
+#pragma unroll
+      for (int j = 0; j < kBigPer; ++j) {
+        const int p = p0 + j;
+        vq[j] = 0;
+        if (j < per && p < m) {
+          const uint32_t kj = sk[p];
+          const uint32_t vv = sv[p];
+          vq[j] = vv;
+          if (p > 0 && prev < kj) bnd |= 1u << j;
+          prev = kj;
+          const uint32_t wj = vv & 0x7FFFFFFu;
+          cols[(int)(vv >> 27) * kColStride + me] += wj;
+          tn += wj;
+        }
+      }
+    }
+    cols[C * kColStride + me] = tn;
+    __syncthreads();
+    for (int c = warp; c <= C; c += kBigWarps) {
+      uint32_t* col = cols + c * kColStride + 8 * lane + (lane >> 2);
+      uint32_t x[8];
+      uint32_t run = 0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        x[i] = run;
+        run += col[i];
+      }
+      uint32_t inc = run;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += y;
+      }
+      const uint32_t base_c = carry[c] + inc - run;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) col[i] = base_c + x[i];
+      const uint32_t total = __shfl_sync(kFull, inc, 31);
+      __syncwarp();
+      if (lane == 0) carry[c] += total;
+    }
+    __syncthreads();
+    long long run_n = (long long)cols[C * kColStride + me];
+    long long Q = 0, hl = 0, hr = 0;
+    bool haveQ = false;
+#pragma unroll 1
+    for (int j = 0; j < per; ++j) {
+      const uint32_t vv = vq[0];
+#pragma unroll
+      for (int k = 0; k + 1 < kBigPer; ++k) vq[k] = vq[k + 1];
+      const int labj = (int)(vv >> 27);
+      const int wj = (int)(vv & 0x7FFFFFFu);
+      const long long nr = (long long)nd.n - run_n;
+      if (((bnd >> j) & 1u) && run_n >= ml && nr >= ml) {
+        if (!haveQ) {
+          Q = entropy_q_u<2 * CW>(
+              H, C, run_n, nr, [&](int c) { return (long long)cols[c * kColStride + me]; },
+              [&](int c) { return (long long)nt[c]; });
+          hl = __ldg(H + run_n);
+          hr = __ldg(H + nr);
+          haveQ = true;
+        }
+        if (nb.offer(prior - Q, p0 + j, nd.n)) {
+          bnl = run_n;
+#pragma unroll
+          for (int c = 0; c < CW; ++c) {
+            const unsigned long long lo = 2 * c < C ? cols[2 * c * kColStride + me] : 0u;
+            const unsigned long long hi = 2 * c + 1 < C ? cols[(2 * c + 1) * kColStride + me] : 0u;
+            bL[c] = lo | (hi << 32);
+          }
+        }
+      }
+      uint32_t* cl = cols + labj * kColStride + me;
+      const long long lc = (long long)*cl;
+      if (haveQ && (bnd >> (j + 1)) != 0u) {
+        const long long rc = (long long)nt[labj] - lc;
+        const long long hl1 = __ldg(H + run_n + wj), hr1 = __ldg(H + nr - wj);
+        Q += (hl1 - hl) + (hr1 - hr) - (__ldg(H + lc + wj) - __ldg(H + lc)) -
+             (__ldg(H + rc - wj) - __ldg(H + rc));
+        hl = hl1;
+        hr = hr1;
+      }
+      *cl = (uint32_t)(lc + wj);
+      run_n += wj;
+    }
+  }
+  *out_g = nb.gain(nd.n);
+  *out_p = nb.p;
+  *out_nl = bnl;
+#pragma unroll
+  for (int c = 0; c < CW; ++c) outL[c] = bL[c];
+}
+
 // Boundary scan of a sorted regression item, whose values index eq, the
 // entries' packed (target, weight) words; `per` (1..8) consecutive elements a
 // thread per tile as above.  Out of line, so that its registers do not weigh
@@ -515,16 +657,27 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
   __shared__ float s_g[kBigWarps];
   __shared__ int s_p[kBigWarps];
   __shared__ long long s_prior;
+  __shared__ int s_item[2];
+  __shared__ int s_nt[kMaxClasses];
   const LevelArgs& a = b.L;
   const int nnodes = b.phase == 1 ? b.nbig : *b.nretry;
-  const long long nitems = (long long)nnodes * b.tries_per_node;
+  const int nitems = nnodes * b.tries_per_node;
   uint32_t* k1 = b.slot + (long long)blockIdx.x * 4 * b.slot_stride;
   uint32_t* v1 = k1 + b.slot_stride;
   uint32_t* k2 = v1 + b.slot_stride;
   uint32_t* v2 = k2 + b.slot_stride;
-  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const int ni = (int)(it / b.tries_per_node);
-    const int ts = (int)(it % b.tries_per_node);
+  int* ctr = b.item_ctr + (b.phase - 1);
+  // Items are handed out one at a time as CTAs become free: nodes differ in
+  // size, and a fixed stride over the items left some CTAs with several times
+  // the work of others.  The item number alternates between two words, so
+  // the next fetch never overwrites a word that a thread may still read.
+  for (int round = 0;; ++round) {
+    if (threadIdx.x == 0) s_item[round & 1] = atomicAdd(ctr, 1);
+    __syncthreads();
+    const int it = s_item[round & 1];
+    if (it >= nitems) break;
+    const int ni = it / b.tries_per_node;
+    const int ts = it % b.tries_per_node;
     const int node = b.phase == 1 ? b.big[ni] : b.retry[ni];
     const LNode nd = a.nodes[node];
     const ProbDesc& P = a.probs[nd.prob];
@@ -539,6 +692,7 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     const float* xf = P.X + (long long)f * P.N;
     if (threadIdx.x == 0 && P.task == 0)
       s_prior = entropy_prior(a.H, nd.n, P.C, [&](int c) { return (long long)ncnt[c]; });
+    if (P.task == 0 && threadIdx.x < P.C) s_nt[threadIdx.x] = ncnt[threadIdx.x];
     // keys (and, for classification, the packed label | weight values) with
     // eight gathers in flight per thread; the keys' OR / AND and the digit
     // histograms of their significant bytes on the way
@@ -564,7 +718,6 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
         if (act) {
           k = rk ? __ldg(rk + rr[j]) : orderable(__ldg(xf + rr[j]));
           k1[i] = k;
-          v1[i] = packed ? __ldg(pv + i) : (uint32_t)i;
           o |= k;
           an &= k;
         }
@@ -595,8 +748,17 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
       }
       diff = oo ^ aa;
     }
-    // S.red is written again only after the sort's and the scan's barriers
-    const bool in2 = big_sort(k1, v1, k2, v2, m, diff, S);
+    // S.red is written again only after the sort's and the scan's barriers.
+    // The values (packed label and weight, or the entry index for regression)
+    // enter with the first pass; keys that are all equal need no pass and
+    // have their values copied.
+    bool in2 = false;
+    if (diff != 0) {
+      in2 = big_sort(k1, v1, k2, v2, packed ? pv : nullptr, m, diff, S);
+    } else {
+      for (int i = threadIdx.x; i < m; i += kBigBlock) v1[i] = packed ? pv[i] : (uint32_t)i;
+      __syncthreads();
+    }
     const uint32_t* sk = in2 ? k2 : k1;
     const uint32_t* sv = in2 ? v2 : v1;
     float g;
@@ -604,7 +766,13 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     long long nl, sl = 0;
     unsigned long long L[CW];
     if (packed) {
-      big_boundary_items<CW>(sk, sv, m, nd, P, ncnt, a.H, s_prior, S.scan64, &g, &p, &nl, L);
+      if constexpr (CW >= 2 && CW <= 5) {
+        static_assert((2 * CW + 1) * (kColStride + 1) <= 2 * kBigTile, "columns fit the tiles");
+        big_boundary_cols<CW>(sk, sv, m, kBigPer, nd, P.C, max(1, P.min_leaf), a.H, s_prior,
+                              s_nt, S.tile, &g, &p, &nl, L);
+      } else {
+        big_boundary_items<CW>(sk, sv, m, nd, P, ncnt, a.H, s_prior, S.scan64, &g, &p, &nl, L);
+      }
     } else {
       big_boundary_reg(sk, sv, b.pq + nd.ebeg, m, kBigPer, nd.n, nd.sum, max(1, P.min_leaf), P.S,
                        P.N, S.scan64, &g, &p, &nl, &sl);
@@ -746,6 +914,7 @@ __global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(Lev
   __shared__ long long s_prior;
   __shared__ int s_scan[kBigWarps];
   __shared__ int s_next;
+  __shared__ int s_nt[kMaxClasses];
   extern __shared__ __align__(16) unsigned char dsm[];
   const int cap = a.smem_cap;
   uint32_t* k1 = (uint32_t*)dsm;
@@ -780,6 +949,7 @@ __global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(Lev
     }
     if (threadIdx.x == 0 && packed)
       s_prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
+    if (packed && threadIdx.x < C) s_nt[threadIdx.x] = ncnt[threadIdx.x];
     __syncthreads();
     int t = 0;
     while (true) {
@@ -834,7 +1004,13 @@ __global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(Lev
       int p;
       long long nl, sl = 0;
       unsigned long long L[CW];
-      if (packed) {
+      bool cols_scan = false;
+      if constexpr (CW >= 2 && CW <= 5) cols_scan = (C + 1) * (kColStride + 1) <= 2 * cap;
+      if (packed && cols_scan) {
+        // the class columns in the sort buffers the sorted pairs are not in
+        big_boundary_cols<CW>(sk, sv, m, per, nd, C, max(1, P.min_leaf), a.H, s_prior, s_nt,
+                              in2 ? k1 : k2, &g, &p, &nl, L);
+      } else if (packed) {
         big_boundary<CW, false>(sk, sv, m, per, nd, P, ncnt, a.H, s_prior, scan64, &g, &p, &nl, L);
       } else {
         big_boundary_reg(sk, sv, q_e, m, per, nd.n, nd.sum, max(1, P.min_leaf), P.S, P.N, scan64,

@@ -535,7 +535,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
         slot_stride > 0 && any_cls ? (uint32_t*)alloc(sizeof(uint32_t) * total_slots) : nullptr;
     long long* big_pq =
         slot_stride > 0 && any_reg ? (long long*)alloc(sizeof(long long) * total_slots) : nullptr;
-    int* d_nretry = (int*)alloc(sizeof(int));
+    // [0] retry count of the big-node search, [1..2] its item counters per phase
+    int* d_nretry = (int*)alloc(sizeof(int) * 3);
     ProbDesc* d_probs = (ProbDesc*)alloc(sizeof(ProbDesc) * nprob);
     DML_CK(cudaMemcpyAsync(d_probs, hp.data(), sizeof(ProbDesc) * nprob, cudaMemcpyHostToDevice, s));
     std::vector<int> tree_prob(total_trees);
@@ -664,14 +665,14 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           b.big_index = big_index.p;
           b.pv = big_pv;
           b.pq = big_pq;
-          DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
+          b.item_ctr = d_nretry + 1;
           b.L.stats = d_stats + 4 + 4 * q;
           DML_CK(cudaEventRecord(qev[q][0], s));
           const int chunk = plain ? kPlainChunk : nb;
           for (int off = 0; off < nb; off += chunk) {
             b.big = qlist[q].p + off;
             b.nbig = std::min(chunk, nb - off);
-            DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int), s));
+            DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int) * 3, s));
             launch_big(CW, b, 1, big_grid, std::min(b.nbig, 65535), max_mand, s);
             launch_big(CW, b, 2, big_grid, std::min(b.nbig, 65535), std::max(1, max_opt), s);
             st.launches += 5;

@@ -81,6 +81,12 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
     }
     Cand best;
     best.valid = 0;
+    // RF classification with value ranks: a candidate carries the ranks on both
+    // sides of its boundary (in suml, a regression field) and its threshold is
+    // read from the value table once per node, after the try loop: tries of
+    // one feature give one candidate, so the threshold never decides between
+    // tries.  The entries' values are then never gathered during the search.
+    const bool defer_thr = P.algo == 0 && P.task == 0 && P.rank != nullptr && P.N <= (1ll << 26);
     // the features of tries 0 .. 31, computed by the group's lanes at once
     constexpr int NT = 32 / G;
     const int ntry = P.n_mand + P.n_opt;
@@ -102,7 +108,7 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
       // RF with value ranks: rank << 5 | group lane as one 32-bit sort key
       // (invalid lanes sort last with their own lane index)
       const bool r32 = P.algo == 0 && P.rank != nullptr && P.N <= (1ll << 26);
-      const float xv = valid ? __ldg(xf + row) : 0.0f;
+      const float xv = valid && !defer_thr ? __ldg(xf + row) : 0.0f;
       Cand cd;
       cd.f = f;
       if (P.algo == 1) {  // ERT: sample s is held by lane s % G, slot s / G
@@ -189,9 +195,9 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
         const int ke = __shfl_sync(gm, k, idx, G);
         const int we = __shfl_sync(gm, w, idx, G);
         const long long qe = __shfl_sync(gm, qv, idx, G);
-        const float xe = __shfl_sync(gm, xv, idx, G);
+        const float xe = defer_thr ? 0.0f : __shfl_sync(gm, xv, idx, G);
         const uint32_t prevk = __shfl_up_sync(gm, key, 1, G);
-        const float prevx = __shfl_up_sync(gm, xe, 1, G);
+        const float prevx = defer_thr ? 0.0f : __shfl_up_sync(gm, xe, 1, G);
         const long long nl = grp_excl_scan<G, long long>(we, gl, gm);
         const long long nr = (long long)nd.n - nl;
         bool bnd = gl > 0 && gl < m && prevk < key && nl >= ml && nr >= ml;
@@ -234,17 +240,25 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
           }
         }
         const int src = bp >= 0 ? bp : 0;
-        const float xa = __shfl_sync(gm, prevx, src, G);
-        const float xb = __shfl_sync(gm, xe, src, G);
         const long long nlb = __shfl_sync(gm, nl, src, G);
         const long long slb = __shfl_sync(gm, sl, src, G);
+        float thr = 0.0f;
+        long long ranks = 0;
+        if (defer_thr) {
+          ranks = ((long long)__shfl_sync(gm, prevk, src, G) << 32) |
+                  (long long)__shfl_sync(gm, key, src, G);
+        } else {
+          const float xa = __shfl_sync(gm, prevx, src, G);
+          const float xb = __shfl_sync(gm, xe, src, G);
+          thr = midpoint_threshold(xa, xb);
+        }
         if (bp >= 0) {
           cd.valid = 1;
           cd.gain = bg;
-          cd.thr = midpoint_threshold(xa, xb);
+          cd.thr = thr;
           cd.nl_e = bp;
           cd.nl = (int)nlb;
-          cd.suml = slb;
+          cd.suml = defer_thr ? ranks : slb;
         } else {
           cd.valid = 0;
           cd.gain = -FLT_MAX;
@@ -273,6 +287,12 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
     if (!best.valid) {
       if (gl == 0) write_leaf(a.res, node);
       continue;
+    }
+    if (defer_thr) {
+      const float* vf = P.vals + (long long)best.f * P.N;
+      best.thr = midpoint_threshold(__ldg(vf + (uint32_t)((unsigned long long)best.suml >> 32)),
+                                    __ldg(vf + (uint32_t)best.suml));
+      best.suml = 0;
     }
     if (gl == 0) write_result(a.res, a.res_cnt, a.Cmax, node, best, nullptr, 0);
     // stable partition with one ballot; the left class counts of the split

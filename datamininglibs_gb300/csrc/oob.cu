@@ -263,8 +263,8 @@ extern "C" dml_status dml_oob_estimate(const dml_forest* f, const dml_fit_desc* 
       out->pairs_sq_err = h[1];
       out->rows_sq_err = h[3];
     }
-  } catch (const CudaError&) {
-    st = DML_ERR_CUDA;
+  } catch (const CudaError& e) {
+    st = e.e == cudaErrorMemoryAllocation ? DML_ERR_OOM : DML_ERR_CUDA;
   } catch (const InvalidArg&) {
     st = DML_ERR_INVALID_ARG;
   }

@@ -434,6 +434,7 @@ class Server:
         _check(lib().dml_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
         self._keep = {}
+        self._inflight = {}  # request id -> (samples, out): alive until the request is done
 
     def add_forest(self, forest):
         fid = ctypes.c_int32()
@@ -442,9 +443,13 @@ class Server:
         return fid.value
 
     def submit(self, forest_id, X, out):
+        """Queues X (feature-major [F, n], host) for prediction into out ([n, width],
+        host).  The server reads X and writes out after submit returns; both
+        are kept referenced here until poll or wait reports the request done."""
         rid = ctypes.c_int64()
         _check(lib().dml_server_submit(self._h, forest_id, X.ctypes.data, X.shape[1],
                                        out.ctypes.data, ctypes.byref(rid)))
+        self._inflight[rid.value] = (X, out)
         return rid.value
 
     def poll(self, rid):
@@ -452,12 +457,16 @@ class Server:
         st = lib().dml_server_poll(self._h, rid, ctypes.byref(lat))
         if st == 6:
             return None
+        self._inflight.pop(rid, None)
         _check(st)
         return lat.value
 
     def wait(self, rid):
         lat = ctypes.c_double()
-        _check(lib().dml_server_wait(self._h, rid, ctypes.byref(lat)))
+        st = lib().dml_server_wait(self._h, rid, ctypes.byref(lat))
+        if st != 4:  # a timed-out request may still be read and written
+            self._inflight.pop(rid, None)
+        _check(st)
         return lat.value
 
     def stats(self):

@@ -109,10 +109,12 @@ def test_server_creation_survives_failures(dml, monkeypatch):
         return dml.Server(hbm_budget_bytes=64 << 20, max_batch_rows=4096, n_streams=2,
                           max_wait_us=0, small_rows=256)
 
+    Xs = np.ascontiguousarray(X[:, :300])  # must stay valid until the request completes
+
     def check(srv):
         fid = srv.add_forest(f)
         out = np.zeros((300, 2), np.float32)
-        srv.wait(srv.submit(fid, np.ascontiguousarray(X[:, :300]), out))
+        srv.wait(srv.submit(fid, Xs, out))
         srv.close()
         assert np.array_equal(out, want)
 

@@ -472,3 +472,46 @@ def test_bulk_predict_in_tree_passes_matches_oracle(dml, monkeypatch, task, pass
     nodes, probs = f.export()
     _assert_same_model(m, nodes, probs)
     assert np.array_equal(f.predict(X), oracle.predict(m, X))
+
+
+def _large_node_case(kind):
+    rng = np.random.default_rng(77)
+    if kind == "cls_10":
+        X, y = synth.rf_multiclass(40000, 12, n_classes=10, n_int=3, seed=78)
+        return X, y, dict(algo=0, n_trees=4, K=4, max_depth=10, min_node_size=5, min_leaf=2,
+                          n_classes=10, seed=4)
+    if kind == "cls_ties_missing":
+        X, y = synth.rf_multiclass(36000, 10, n_classes=3, n_int=2, seed=79)
+        X[0] = np.round(X[0], 1)                       # many ties
+        X[1, rng.random(X.shape[1]) < 0.2] = -FLT_MAX  # missing values, go left
+        X[2, rng.random(X.shape[1]) < 0.3] = -0.0      # signed zeros beside +0
+        X[2, rng.random(X.shape[1]) < 0.3] = 0.0
+        return X, y, dict(algo=0, n_trees=3, K=10, max_depth=9, min_node_size=5,
+                          n_classes=3, seed=5)
+    if kind == "cls_balanced_rare_class":
+        X, y = synth.rf_multiclass(40000, 8, n_classes=3, n_int=2, seed=80)
+        y = np.where(y == 2, 1, y).astype(np.float32)
+        y[rng.choice(y.size, 25, replace=False)] = 2   # 25 rows of class 2: weights far above 15
+        return X, y, dict(algo=0, n_trees=3, K=4, max_depth=8, min_node_size=5, n_classes=3,
+                          seed=6, balanced=1)
+    X, y = synth.rf_regression(40000, 10, seed=81)
+    X[3] = np.round(X[3], 2)
+    return X, y, dict(algo=0, task=1, n_trees=3, K=5, max_depth=12, min_node_size=5,
+                      min_leaf=3, seed=7)
+
+
+@pytest.mark.parametrize("kind", ["cls_10", "cls_ties_missing", "cls_balanced_rare_class",
+                                  "reg_ties"])
+def test_large_node_edge_cases_match_oracle(dml, kind):
+    """Nodes of tens of thousands of entries (far above the shared-memory cap,
+    searched as per-try items) with many ties, missing values, signed zeros,
+    ten classes, regression, and bootstrap weights far above 15 (a balanced
+    bootstrap with a 25-row class): trees, payloads, gains and votes equal the
+    oracle's."""
+    X, y, kw = _large_node_case(kind)
+    m, f, nodes, probs = _fit_both(dml, X, y, **kw)
+    _assert_same_model(m, nodes, probs, kind)
+    g = f.gains()
+    split = nodes[:, 1] > 0
+    assert np.array_equal(g[split].view(np.uint32), m.gains32[split].view(np.uint32)), kind
+    assert np.array_equal(f.predict(X), oracle.predict(m, X)), kind
