@@ -109,6 +109,28 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def host_link_rate(torch, mib=256):
+    """Copy rate between pinned host memory and the device (GB/s, CUDA events on
+    one 256 MiB copy each way).  The end-to-end fit and the serving leg move
+    their samples, models and requests over this link, and its rate has varied
+    between boxes and over time (other jobs share the host), so it is reported
+    beside the numbers that depend on it."""
+    n = mib << 18
+    d = torch.empty(n, dtype=torch.float32, device="cuda")
+    h = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    h.fill_(1.0)
+    out = {}
+    for key, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        dst.copy_(src, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        out[key] = round(n * 4 / (a.elapsed_time(b) * 1e6), 1)
+    return out
+
+
 def traffic_from_profile(kernel):
     """DRAM bytes per tried entry of a search kernel, measured by ncu on the
     200k x 64 case (profiles/search_kernels_rf_multiclass.md, lines
@@ -382,7 +404,9 @@ def serve_leg(dml, torch, stream, c2_forest, c4_forests, c4_probs):
             "p99_ms_le4k": float(np.percentile(lat[small], 99))}
     bursts = []
     for rep in range(3):
+        link = host_link_rate(torch)
         reqs, b = burst(5 + rep)
+        b["host_link_GBps_before"] = link
         bursts.append(b)
     st = srv.stats()
     srv.close()
@@ -529,6 +553,7 @@ def run_ours(args, w):
     nbuf = torch.empty((finfo.n_nodes, 5), dtype=torch.int32, pin_memory=True).numpy()
     pbuf = torch.empty(finfo.n_probs, dtype=torch.float32, pin_memory=True).numpy()
     e2e_steps = max(1, min(args.steps, 3))
+    link_before = host_link_rate(torch)
     barrier()
     t0 = time.perf_counter()
     e2e_nodes = 0
@@ -541,6 +566,7 @@ def run_ours(args, w):
         f.free()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    link_after = host_link_rate(torch)
     h2d = X.nbytes + y.nbytes
 
     extras = {}
@@ -611,6 +637,8 @@ def run_ours(args, w):
         "search_kernels": queues,
         "e2e": {"value": e2e_nodes / e2e_s, "unit": "nodes/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h // e2e_steps},
+        "host_link_GBps": {"before_e2e": link_before, "after_e2e": link_after,
+                           "note": "pinned host <-> device copy rate, 256 MiB each way"},
         "gpu_launches": launches,
         "clocks": clocks,
     }
