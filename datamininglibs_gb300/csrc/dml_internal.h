@@ -73,6 +73,16 @@ struct PNode {
   int pad;
 };
 
+// Compact predict layout for bulk prediction, one 8-byte load per node, same
+// node indices as PNode.  Internal: w = (offset of the children from the node
+// << fbits) | feature; leaf: w = (voted class << fbits) | 2^fbits - 1; t = the
+// split point or the regression leaf value.  Built when every feature and
+// child offset fits (fbits = bits of the feature count).
+struct PNode8 {
+  uint32_t w;
+  float t;
+};
+
 // Per-level, per-forest segment of the level list (for the final gather).
 struct Seg {
   long long node_pos;   // position in the node log

@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "../../include/dml.h"
@@ -26,6 +27,12 @@ struct dml_forest {
   float* probs = nullptr;              // device
   long long n_probs = 0;
   dml::PNode* pnodes = nullptr;        // device, predict layout
+  // device, compact predict layout (null when it does not fit or before the
+  // first bulk prediction, which builds it) and its feature bits
+  mutable dml::PNode8* pnodes8 = nullptr;
+  mutable int p8_bits = 0;
+  mutable bool p8_tried = false;
+  mutable std::mutex p8_mu;
   float* gains = nullptr;              // device, FP32 gain per node (NaN for leaves); null
                                        // for forests not fitted by this engine
   dml::ForestBlock* block = nullptr;   // set when the three arrays live in a shared block
@@ -59,6 +66,7 @@ void build_nlogn_table(long long nmax, long long* out);
 int quant_scale_from_max(float maxabs, long long n);
 
 dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s);
+void forest_build_pnodes8(const dml_forest* f, cudaStream_t s);
 
 // Largest RF node (entries) the shared-memory search kernel can hold, and the
 // default: with buffers of 2048 entries (48 KB) three CTAs fit an SM.

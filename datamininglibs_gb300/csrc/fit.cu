@@ -956,6 +956,41 @@ dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s) {
   return DML_OK;
 }
 
+// The compact layout, built once per forest by its first bulk prediction,
+// when the features and every child offset fit 32 bits; a word past the
+// nodes flags an offset that does not (the layout is then dropped, and bulk
+// prediction walks the 16-byte one).  Synchronises s.
+void forest_build_pnodes8(const dml_forest* f, cudaStream_t s) {
+  std::lock_guard<std::mutex> lock(f->p8_mu);
+  if (f->p8_tried) return;
+  f->p8_tried = true;
+  const int g = (int)std::min<long long>(8192, (f->n_nodes + 255) / 256 + 1);
+  int fb = 1;
+  while ((1 << fb) - 1 < f->n_features) ++fb;
+  if (fb <= 16 && f->n_nodes > 0 && f->n_classes < (1 << (32 - fb)) &&
+      cudaMalloc(&f->pnodes8, sizeof(PNode8) * (f->n_nodes + 1)) == cudaSuccess) {
+    int* flag = reinterpret_cast<int*>(f->pnodes8 + f->n_nodes);
+    int h_flag = 1;
+    if (cudaMemsetAsync(flag, 0, sizeof(int), s) == cudaSuccess) {
+      k_to_pnodes8<<<g, 256, 0, s>>>(f->pnodes, f->n_nodes, fb, f->pnodes8, flag);
+      if (cudaGetLastError() != cudaSuccess ||
+          cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess)
+        h_flag = 1;
+    }
+    if (h_flag) {
+      cudaGetLastError();
+      cudaFree(f->pnodes8);
+      f->pnodes8 = nullptr;
+    } else {
+      f->p8_bits = fb;
+    }
+  } else {
+    cudaGetLastError();
+    f->pnodes8 = nullptr;
+  }
+}
+
 static dml_status fit_entry(const dml_fit_desc* descs, int n, dml_forest** out, void* stream,
                             bool plain) {
   clear_error();

@@ -805,6 +805,31 @@ __global__ void k_to_pnodes(const ClassifyNode* nodes, long long n, const float*
   }
 }
 
+// Compact predict layout (PNode8) from the 16-byte one; *bad is set when a
+// child offset does not fit the bits above the feature field.
+__global__ void k_to_pnodes8(const PNode* in, long long n, int fbits, PNode8* out, int* bad) {
+  const uint32_t marker = (1u << fbits) - 1u;
+  const long long lim = 1ll << (32 - fbits);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const PNode p = in[i];
+    PNode8 q;
+    q.t = p.t;
+    if (p.a >= 0) {
+      const long long off = (long long)p.a - i;
+      if (off <= 0 || off >= lim) {
+        atomicExch(bad, 1);
+        q.w = 0;
+      } else {
+        q.w = ((uint32_t)off << fbits) | (uint32_t)p.b;
+      }
+    } else {
+      q.w = ((uint32_t)p.b << fbits) | marker;
+    }
+    out[i] = q;
+  }
+}
+
 #endif  // DML_SEARCH_CW
 
 }  // namespace dml

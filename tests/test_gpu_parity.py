@@ -457,7 +457,9 @@ def test_forest_file_roundtrip(dml, tmp_path):
 def test_bulk_predict_in_tree_passes_matches_oracle(dml, monkeypatch, task, pass_mb):
     """Predictions of 70,000 rows (the bulk path: passes over blocks of trees,
     votes and regression sums carried between passes) equal the oracle's, bit
-    for bit; DML_PREDICT_PASS_MB=1 forces a pass per few trees."""
+    for bit, over the compact 8-byte node layout and, with DML_PREDICT_NODE16
+    set, over the 16-byte one; DML_PREDICT_PASS_MB=1 forces a pass per few
+    trees."""
     if pass_mb:
         monkeypatch.setenv("DML_PREDICT_PASS_MB", pass_mb)
     if task == 0:
@@ -471,7 +473,10 @@ def test_bulk_predict_in_tree_passes_matches_oracle(dml, monkeypatch, task, pass
     f = dml.fit(X, y, **kw)
     nodes, probs = f.export()
     _assert_same_model(m, nodes, probs)
-    assert np.array_equal(f.predict(X), oracle.predict(m, X))
+    want = oracle.predict(m, X)
+    assert np.array_equal(f.predict(X), want)
+    monkeypatch.setenv("DML_PREDICT_NODE16", "1")
+    assert np.array_equal(f.predict(X), want)
 
 
 def _large_node_case(kind):
