@@ -103,9 +103,10 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles(const PredTile* __r
 
 // Small lane: the tile's 16 rows are staged in shared memory (from device
 // staging or straight from the caller's pinned buffer), then 8 threads per row
-// walk trees g, g+8, ...; votes meet in shared memory (integer counts,
-// order-free); regression leaf values are kept per tree and summed in tree
-// order by one thread.
+// walk trees g, g+8, ..., four of them in lockstep (four node loads in
+// flight: a request's latency is the chain of dependent node loads); votes
+// meet in shared memory (integer counts, order-free); regression leaf values
+// are kept per tree and summed in tree order by one thread.
 __global__ void __launch_bounds__(kTileRows) k_predict_tiles_split(
     const PredTile* __restrict__ tiles) {
   extern __shared__ int sm[];  // xs [F][kSplitStride], then votes [kSplitRows][C] or values
@@ -125,17 +126,35 @@ __global__ void __launch_bounds__(kTileRows) k_predict_tiles_split(
   __syncthreads();
   float* vals = reinterpret_cast<float*>(acc) + r * t.n_trees;
   if (act) {
-    for (int k = g; k < t.n_trees; k += kSplit) {
-      int4 p = __ldg(reinterpret_cast<const int4*>(t.nodes) + k);
-      while (p.x >= 0) {
-        const float x = xs[p.y * kSplitStride + r];
-        const int nx = goes_left(x, __int_as_float(p.z)) ? p.x : p.x + 1;
-        p = __ldg(reinterpret_cast<const int4*>(t.nodes) + nx);
+    const int4* nd = reinterpret_cast<const int4*>(t.nodes);
+    for (int k0 = g; k0 < t.n_trees; k0 += 4 * kSplit) {
+      int4 p[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = k0 + j * kSplit;
+        p[j] = k < t.n_trees ? __ldg(nd + k) : make_int4(-1, 0, 0, 0);
       }
-      if (t.task == 0)
-        atomicAdd(&acc[r * t.C + p.y], 1);
-      else
-        vals[k] = __int_as_float(p.z);
+      bool more = true;
+      while (more) {
+        more = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (p[j].x >= 0) {
+            const float x = xs[p[j].y * kSplitStride + r];
+            p[j] = __ldg(nd + (goes_left(x, __int_as_float(p[j].z)) ? p[j].x : p[j].x + 1));
+            more = more || p[j].x >= 0;
+          }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = k0 + j * kSplit;
+        if (k < t.n_trees) {
+          if (t.task == 0)
+            atomicAdd(&acc[r * t.C + p[j].y], 1);
+          else
+            vals[k] = __int_as_float(p[j].z);
+        }
+      }
     }
   }
   __syncthreads();
