@@ -33,9 +33,13 @@ __device__ __forceinline__ T grp_sum(T v, unsigned gm) {
 }
 
 template <int CW, int G>
-// Three resident CTAs per SM (80 registers): the extra warps hide the shuffle
-// latency of the sort and scans better than 128 registers without spills.
-__global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
+// Five resident CTAs per SM (51 registers, some spilled): the group scans and
+// sorts wait on shuffle latency, and the extra warps hide it better than
+// fewer at more registers (the C2 group classes at 3 / 4 / 5 CTAs per SM:
+// 135 / 115 / 106 ms).  The node's class counts are read from global memory
+// where the ERT gain needs them rather than held in registers.  Eight or more
+// packed class words keep three CTAs (80 registers).
+__global__ void __launch_bounds__(256, CW >= 8 ? 3 : 5) k_group_nodes(LevelArgs a) {
   constexpr int NPW = 32 / G;                 // nodes per warp
   constexpr int NS = (10 + G - 1) / G;        // ERT samples per lane
   const int lane = threadIdx.x & 31;
@@ -64,9 +68,6 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
     const int k = (valid && P.task == 0) ? __ldg(P.lab + row) : -1;
     const long long qv = (valid && P.task == 1) ? __ldg(P.q + row) : 0;
     long long prior = 0;
-    int Nt[2 * CW];
-#pragma unroll
-    for (int c = 0; c < 2 * CW; ++c) Nt[c] = (P.task == 0 && c < C) ? ncnt[c] : 0;
     if (P.task == 0) prior = entropy_prior(a.H, nd.n, C, [&](int c) { return (long long)ncnt[c]; });
     // RF classification: h(n), the class total of each lane's entry and the
     // bit planes of the group's largest weight, fixed across tries
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(256, 3) k_group_nodes(LevelArgs a) {
             Lc[c] = c < C ? __popc(__ballot_sync(gm, k == c) & lm) : 0;
           cd.gain = cd.valid ? entropy_gain_u<2 * CW>(
                                    a.H, prior, C, nl, nr, [&](int c) { return (long long)Lc[c]; },
-                                   [&](int c) { return (long long)Nt[c]; })
+                                   [&](int c) { return (long long)__ldg(ncnt + c); })
                              : -FLT_MAX;
         } else {
           long long sl = grp_sum<G, long long>(left ? qv : 0, gm);

@@ -83,11 +83,17 @@ constexpr int warp_rf_wpb() {
   return E >= 16 ? 2 : 8;
 }
 
-// Resident blocks per SM the registers are sized for: 16 warps (128 registers
-// a thread; a 512-entry block's 25 KB of shared memory also allows eight).
-template <int E>
+// Resident blocks per SM the registers are sized for, by measurement on the
+// 1M x 128 fit (class times at 16 / 24 / 32 warps per SM): E = 2 at 32 warps
+// (64 registers; 61.4 / 47.7 / 43.8 ms), E = 4 at 24 (85; 45.4 / 38.6 /
+// 38.7), E = 8 at 24 (85; 38.2 / 37.6 / 60.1), E = 16 at 16 (128; 58.1 /
+// 76.3 / 82.3).  More warps hide the shuffle latency of the sorts and scans
+// until the spills of the larger register sets cost more than they hide.
+// Eight or more packed class words keep 16 warps (128 registers): their class
+// counts alone take 16 or 32 registers.
+template <int E, int CW>
 constexpr int warp_rf_min_blocks() {
-  return 16 / warp_rf_wpb<E>();
+  return (CW >= 8 ? 16 : E == 2 ? 32 : E == 16 ? 16 : 24) / warp_rf_wpb<E>();
 }
 
 struct RegScan {
@@ -173,7 +179,7 @@ static __device__ __forceinline__ RegScan warp_reg_scan(const unsigned long long
 }
 
 template <int E, int CW>
-__global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E>())
+__global__ void __launch_bounds__(32 * warp_rf_wpb<E>(), warp_rf_min_blocks<E, CW>())
     k_warp_rf(LevelArgs a) {
   constexpr int M = 32 * E;
   constexpr int WPB = warp_rf_wpb<E>();
