@@ -14,8 +14,11 @@
 
 namespace dml {
 
+// Three resident blocks per SM (24 warps, 85 registers, some spilled): on the
+// 256 uneven forests the class took 15.0 ms at two blocks, 11.8 at three and
+// 11.9 at four.
 template <int E>
-__global__ void __launch_bounds__(256, 2) k_ert_warp(LevelArgs a) {
+__global__ void __launch_bounds__(256, 3) k_ert_warp(LevelArgs a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
