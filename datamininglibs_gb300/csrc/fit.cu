@@ -264,6 +264,10 @@ static const char* const kQueueNames[kNumQ] = {
     "group32", "ert_cta", "rf_smem", "rf_big", "rf_warp64", "rf_warp128",
     "rf_warp256", "group16", "group8", "rf_warp512", "ert_warp256"};
 
+// Fits of at most this many entries (rows drawn into all trees) overlap their
+// node classes' launches.
+constexpr long long kConcurrentClassEntries = 16ll << 20;
+
 static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bool plain,
                                         cudaStream_t s) {
   NvtxRange fit_range("dml fit: %d forest(s)%s", nprob, plain ? ", plain" : "");
@@ -610,6 +614,30 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       DML_CK(cudaEventCreate(&e[0]));
       DML_CK(cudaEventCreate(&e[1]));
     }
+    // On small fits the node classes of a level run on streams of their own:
+    // each node is in one class and writes only its own results and entry
+    // range, so the classes are independent, and their launches overlap where
+    // a level is too small to fill the GPU (the 4601 x 57, 64-tree ERT fit:
+    // 2.4 -> 1.8 ms).  On large fits the classes' kernels compete for SMs and
+    // caches instead (the 1M x 128 fit: 728 -> 826 ms), so they run one after
+    // another on the fit stream, as they do on the plain path and with
+    // DML_SERIAL_CLASSES=1.
+    const char* senv = getenv("DML_SERIAL_CLASSES");
+    const bool concurrent =
+        !plain && !(senv && senv[0] == '1') && total_slots <= kConcurrentClassEntries;
+    cudaStream_t qstream[kNumQ];
+    cudaEvent_t ev_fork, ev_join[kNumQ];
+    DML_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    for (int q = 0; q < kNumQ; ++q) {
+      qstream[q] = s;
+      DML_CK(cudaEventCreateWithFlags(&ev_join[q], cudaEventDisableTiming));
+      if (concurrent) DML_CK(cudaStreamCreateWithFlags(&qstream[q], cudaStreamNonBlocking));
+    }
+    // launch order: the longest classes first, so that the short ones fill
+    // their tails
+    static constexpr int kClassOrder[kNumQ] = {kQRfBig, kQRfSmall, kQRfW16, kQRfW8, kQRfW4,
+                                               kQRfW2,  kQErt,     kQErtW,  kQWarp, kQG16,
+                                               kQG8};
     double queue_ms[kNumQ] = {};
     int queue_launches[kNumQ] = {};
     const char* tenv = getenv("DML_TRACE");
@@ -634,20 +662,27 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       a.smem_cap = tune.smem_cap;
       int qc[kNumQ];
       std::memcpy(qc, h_sum->qcount, sizeof(qc));
+      // the big class's buffers, allocated in stream order on s before the fork
+      if (qc[kQRfBig] > 0) {
+        const int nb = qc[kQRfBig];
+        big_cand.reserve((size_t)nb * kMaxTries, s, false);
+        big_candL.reserve((size_t)nb * kMaxTries * Cmax, s, false);
+        big_partial.reserve((size_t)nb, s, false);
+        big_partialL.reserve((size_t)nb * Cmax, s, false);
+        big_retry.reserve((size_t)nb, s, false);
+        big_index.reserve((size_t)n, s, false);
+      }
       DML_CK(cudaEventRecord(es0, s));
+      if (concurrent) DML_CK(cudaEventRecord(ev_fork, s));
       float qms[kNumQ] = {};
-      for (int q = 0; q < kNumQ; ++q) {
+      for (int q : kClassOrder) {
         if (qc[q] <= 0) continue;
         NvtxRange class_range("dml search %s: %d nodes", kQueueNames[q], qc[q]);
+        cudaStream_t sq = qstream[q];
+        if (concurrent) DML_CK(cudaStreamWaitEvent(sq, ev_fork, 0));
         if (q == kQRfBig) {
           // per-(node, try) items on a persistent grid with per-CTA scratch
           const int nb = qc[q];
-          big_cand.reserve((size_t)nb * kMaxTries, s, false);
-          big_candL.reserve((size_t)nb * kMaxTries * Cmax, s, false);
-          big_partial.reserve((size_t)nb, s, false);
-          big_partialL.reserve((size_t)nb * Cmax, s, false);
-          big_retry.reserve((size_t)nb, s, false);
-          big_index.reserve((size_t)n, s, false);
           BigArgs b;
           b.L = a;
           b.big = qlist[q].p;
@@ -667,39 +702,43 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           b.pq = big_pq;
           b.item_ctr = d_nretry + 1;
           b.L.stats = d_stats + 4 + 4 * q;
-          DML_CK(cudaEventRecord(qev[q][0], s));
+          DML_CK(cudaEventRecord(qev[q][0], sq));
           const int chunk = plain ? kPlainChunk : nb;
           for (int off = 0; off < nb; off += chunk) {
             b.big = qlist[q].p + off;
             b.nbig = std::min(chunk, nb - off);
-            DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int) * 3, s));
-            launch_big(CW, b, 1, big_grid, std::min(b.nbig, 65535), max_mand, s);
-            launch_big(CW, b, 2, big_grid, std::min(b.nbig, 65535), std::max(1, max_opt), s);
+            DML_CK(cudaMemsetAsync(d_nretry, 0, sizeof(int) * 3, sq));
+            launch_big(CW, b, 1, big_grid, std::min(b.nbig, 65535), max_mand, sq);
+            launch_big(CW, b, 2, big_grid, std::min(b.nbig, 65535), std::max(1, max_opt), sq);
             st.launches += 5;
             queue_launches[q] += 5;
-            if (plain) DML_CK(cudaStreamSynchronize(s));
+            if (plain) DML_CK(cudaStreamSynchronize(sq));
           }
-          DML_CK(cudaEventRecord(qev[q][1], s));
-          continue;
-        }
-        LevelArgs aq = a;
-        aq.stats = d_stats + 4 + 4 * q;
-        DML_CK(cudaEventRecord(qev[q][0], s));
-        if (!plain) {
-          aq.work = qlist[q].p;
-          launch_search(CW, q, aq, qc[q], s);
-          ++st.launches;
-          ++queue_launches[q];
+          DML_CK(cudaEventRecord(qev[q][1], sq));
         } else {
-          for (int off = 0; off < qc[q]; off += kPlainChunk) {
-            aq.work = qlist[q].p + off;
-            launch_search(CW, q, aq, std::min(kPlainChunk, qc[q] - off), s);
+          LevelArgs aq = a;
+          aq.stats = d_stats + 4 + 4 * q;
+          DML_CK(cudaEventRecord(qev[q][0], sq));
+          if (!plain) {
+            aq.work = qlist[q].p;
+            launch_search(CW, q, aq, qc[q], sq);
             ++st.launches;
             ++queue_launches[q];
-            DML_CK(cudaStreamSynchronize(s));
+          } else {
+            for (int off = 0; off < qc[q]; off += kPlainChunk) {
+              aq.work = qlist[q].p + off;
+              launch_search(CW, q, aq, std::min(kPlainChunk, qc[q] - off), sq);
+              ++st.launches;
+              ++queue_launches[q];
+              DML_CK(cudaStreamSynchronize(sq));
+            }
           }
+          DML_CK(cudaEventRecord(qev[q][1], sq));
         }
-        DML_CK(cudaEventRecord(qev[q][1], s));
+        if (concurrent) {
+          DML_CK(cudaEventRecord(ev_join[q], sq));
+          DML_CK(cudaStreamWaitEvent(s, ev_join[q], 0));
+        }
       }
       DML_CK(cudaEventRecord(es1, s));
       // -------------------------------------------------- scans
@@ -812,6 +851,11 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     for (auto& e : qev) {
       cudaEventDestroy(e[0]);
       cudaEventDestroy(e[1]);
+    }
+    cudaEventDestroy(ev_fork);
+    for (int q = 0; q < kNumQ; ++q) {
+      cudaEventDestroy(ev_join[q]);
+      if (concurrent) cudaStreamDestroy(qstream[q]);
     }
     long long h_stats[kStatWords];
     DML_CK(cudaMemcpy(h_stats, d_stats, sizeof(h_stats), cudaMemcpyDeviceToHost));
