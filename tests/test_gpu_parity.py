@@ -202,6 +202,22 @@ def test_repeated_fits_bitwise_identical(dml):
         assert np.array_equal(ref[0], again[0]) and np.array_equal(ref[1], again[1])
 
 
+@pytest.mark.parametrize("name", ["rf_cls", "ert_cls"])
+def test_overlapped_node_classes_equal_serial_ones(dml, monkeypatch, name):
+    """Small fits launch a level's node classes on streams of their own; with
+    DML_SERIAL_CLASSES=1 they run one after another.  Same forest, bit for
+    bit, with every node class present (nodes from the root down to a few
+    entries)."""
+    gen, kw = CASES[name]
+    X, y = gen()
+    over = dml.fit(X, y, **kw)
+    monkeypatch.setenv("DML_SERIAL_CLASSES", "1")
+    serial = dml.fit(X, y, **kw)
+    a, b = over.export(), serial.export()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(over.gains().view(np.uint32), serial.gains().view(np.uint32))
+
+
 EDGE = {
     "root_leaf_depth0": dict(max_depth=0),
     "min_node_size_huge": dict(min_node_size=10 ** 6),
