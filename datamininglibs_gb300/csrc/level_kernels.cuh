@@ -35,7 +35,8 @@ __device__ __forceinline__ T grp_sum(T v, unsigned gm) {
 template <int CW, int G>
 // Five resident CTAs per SM (51 registers, some spilled): the group scans and
 // sorts wait on shuffle latency, and the extra warps hide it better than
-// fewer at more registers (the C2 group classes at 3 / 4 / 5 CTAs per SM:
+// fewer at more registers (the group classes of the 1M x 128, 10-class fit
+// at 3 / 4 / 5 CTAs per SM:
 // 135 / 115 / 106 ms).  The node's class counts are read from global memory
 // where the ERT gain needs them rather than held in registers.  Eight or more
 // packed class words keep three CTAs (80 registers).

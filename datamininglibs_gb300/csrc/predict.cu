@@ -276,8 +276,9 @@ __global__ void __launch_bounds__(kPredBlock) k_predict_split8(const PNode8* __r
 }
 
 // Trees per pass: the pass's share of the predict nodes within kPassNodes
-// nodes (or DML_PREDICT_PASS_MB megabytes of them).  On the 128-tree C2
-// forest 16 trees a pass (5.4 M nodes) were fastest with either layout: 8
+// nodes (or DML_PREDICT_PASS_MB megabytes of them).  On the 128-tree forest
+// of the 1M x 128, 10-class fit (43 M nodes, predicting its 1M rows) 16
+// trees a pass (5.4 M nodes) were fastest with either layout: 8
 // trees 105.8, 16 trees 116.6, 24 trees 106.7 M rows/s with 16-byte nodes;
 // 16 trees 144.2, 32 trees 127.8, 64 trees 130.1 M rows/s with 8-byte ones.
 constexpr long long kPassNodes = 6ll << 20;
