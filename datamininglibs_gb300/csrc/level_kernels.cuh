@@ -36,10 +36,10 @@ template <int CW, int G>
 // Five resident CTAs per SM (51 registers, some spilled): the group scans and
 // sorts wait on shuffle latency, and the extra warps hide it better than
 // fewer at more registers (the group classes of the 1M x 128, 10-class fit
-// at 3 / 4 / 5 CTAs per SM:
-// 135 / 115 / 106 ms).  The node's class counts are read from global memory
-// where the ERT gain needs them rather than held in registers.  Eight or more
-// packed class words keep three CTAs (80 registers).
+// took 135 / 115 / 106 ms at 3 / 4 / 5 CTAs per SM).  The node's class
+// counts are read from global memory where the ERT gain needs them rather
+// than held in registers.  Eight or more packed class words keep three CTAs
+// (80 registers).
 __global__ void __launch_bounds__(256, CW >= 8 ? 3 : 5) k_group_nodes(LevelArgs a) {
   constexpr int NPW = 32 / G;                 // nodes per warp
   constexpr int NS = (10 + G - 1) / G;        // ERT samples per lane
