@@ -272,8 +272,11 @@ struct LevelArgs {
 // the try loop's decision, then the stable partition.
 constexpr int kErtChunk = 16;
 
+// Six resident CTAs per SM (40 registers, no spills): on the 256 uneven
+// forests the class took 13.5 ms at the four CTAs that 64 registers allow,
+// 11.5 at six and 12.5 at eight.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_ert_cta(LevelArgs a) {
+__global__ void __launch_bounds__(BLOCK, 6) k_ert_cta(LevelArgs a) {
   constexpr int NW = BLOCK / 32;
   __shared__ int s_f[kErtChunk];
   __shared__ float s_thr[kErtChunk];
