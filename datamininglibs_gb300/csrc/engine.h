@@ -66,6 +66,11 @@ void build_nlogn_table(long long nmax, long long* out);
 int quant_scale_from_max(float maxabs, long long n);
 
 dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s);
+// Copies `bytes` between a host buffer and device memory on stream s: with
+// SM loads and stores through the host buffer's mapped device pointer when the
+// buffer is pinned and both ends are 16-byte aligned, else by cudaMemcpyAsync.
+cudaError_t copy_host_device(void* dst, const void* src, size_t bytes, bool to_device,
+                             cudaStream_t s);
 void forest_build_pnodes8(const dml_forest* f, cudaStream_t s);
 
 // Largest RF node (entries) the shared-memory search kernel can hold, and the

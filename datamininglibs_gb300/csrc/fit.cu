@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -130,6 +131,43 @@ void dev_free(void* p, cudaStream_t s) {
 // predictions reuse device buffers instead of returning to the driver.  The
 // release threshold is an attribute of each device's own pool, so it is set
 // once per device (the first fit on it).
+// Host <-> device copies of pinned buffers by SMs.  On the GB300 machines the
+// copy engines' rate between pinned host memory and the device has varied
+// over time (other jobs share the host); in one probe it fell from 193-211 to
+// 26-54 GB/s while SM copies through the same buffers' mapped pointers still
+// ran at 104-193 GB/s, and on an unloaded link both ran at 193-210 GB/s.
+__global__ void k_copy16(const int4* __restrict__ src, int4* __restrict__ dst, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+cudaError_t copy_host_device(void* dst, const void* src, size_t bytes, bool to_device,
+                             cudaStream_t s) {
+  if (bytes == 0) return cudaSuccess;
+  const void* host = to_device ? src : dst;
+  void* mapped = nullptr;
+  const size_t body = bytes & ~(size_t)15;
+  const bool aligned = ((uintptr_t)dst % 16 == 0) && ((uintptr_t)src % 16 == 0);
+  if (body == 0 || !aligned ||
+      cudaHostGetDevicePointer(&mapped, const_cast<void*>(host), 0) != cudaSuccess) {
+    cudaGetLastError();  // not pinned (or not mapped): the copy engines
+    return cudaMemcpyAsync(dst, src, bytes,
+                           to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s);
+  }
+  const int4* from = (const int4*)(to_device ? mapped : src);
+  int4* to = (int4*)(to_device ? dst : mapped);
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  const long long n = (long long)(body / 16);
+  const long long grid = std::min<long long>((long long)sms * 4, (n + 511) / 512);
+  k_copy16<<<(unsigned)grid, 512, 0, s>>>(from, to, n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || body == bytes) return e;
+  return cudaMemcpyAsync((char*)dst + body, (const char*)src + body, bytes - body,
+                         to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s);
+}
+
 void init_pool_once() {
   constexpr int kMaxDev = 64;
   static std::once_flag once[kMaxDev];
@@ -410,8 +448,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       if (d.memory == DML_HOST) {
         float* dx = (float*)alloc(sizeof(float) * P.N * P.F);
         float* dy = (float*)alloc(sizeof(float) * P.N);
-        DML_CK(cudaMemcpyAsync(dx, d.samples, sizeof(float) * P.N * P.F, cudaMemcpyHostToDevice, s));
-        DML_CK(cudaMemcpyAsync(dy, d.targets, sizeof(float) * P.N, cudaMemcpyHostToDevice, s));
+        DML_CK(copy_host_device(dx, d.samples, sizeof(float) * P.N * P.F, true, s));
+        DML_CK(copy_host_device(dy, d.targets, sizeof(float) * P.N, true, s));
         H.X = dx;
         H.y = dy;
       }

@@ -512,10 +512,11 @@ dml_status dml_forest_export(const dml_forest* f, void* node_array, float* probs
     set_error("null argument");
     return DML_ERR_INVALID_ARG;
   }
-  if (cudaMemcpy(node_array, f->nodes, sizeof(ClassifyNode) * f->n_nodes, cudaMemcpyDeviceToHost) !=
+  if (copy_host_device(node_array, f->nodes, sizeof(ClassifyNode) * f->n_nodes, false, 0) !=
           cudaSuccess ||
-      cudaMemcpy(probs, f->probs, sizeof(float) * f->n_probs, cudaMemcpyDeviceToHost) !=
-          cudaSuccess) {
+      copy_host_device(probs, f->probs, sizeof(float) * f->n_probs, false, 0) != cudaSuccess ||
+      cudaStreamSynchronize(0) != cudaSuccess) {
+    cudaGetLastError();
     set_error("device to host copy failed");
     return DML_ERR_CUDA;
   }

@@ -169,6 +169,27 @@ def test_export_into_given_buffers(dml):
         f.export(n2, p2.astype(np.float64))
 
 
+def test_pinned_host_buffers_copied_by_sms(dml):
+    """Samples and labels in pinned host memory are uploaded, and a model
+    exported into pinned buffers is downloaded, by SM copies through the
+    buffers' mapped pointers (the samples' and labels' sizes here, 156,052 and
+    12,004 bytes, leave a 4-byte tail for the copy engines): the same forest,
+    bit for bit, as from and into pageable arrays."""
+    torch = pytest.importorskip("torch")
+    X, y = synth.rf_multiclass(3001, 13, n_classes=5, n_int=2, seed=61)
+    kw = dict(algo=0, n_trees=6, K=4, max_depth=12, min_node_size=5, n_classes=5, seed=2)
+    ref = dml.fit(X, y, **kw)
+    rn, rp = ref.export()
+    Xp = torch.from_numpy(X).pin_memory().numpy()
+    yp = torch.from_numpy(y).pin_memory().numpy()
+    f = dml.fit(Xp, yp, **kw)
+    info = f.info()
+    nbuf = torch.empty((info.n_nodes, 5), dtype=torch.int32, pin_memory=True).numpy()
+    pbuf = torch.empty(info.n_probs, dtype=torch.float32, pin_memory=True).numpy()
+    nodes, probs = f.export(nbuf, pbuf)
+    assert np.array_equal(nodes, rn) and np.array_equal(probs, rp)
+
+
 def test_forests_of_one_fit_free_independently(dml):
     """The forests of one fit share one device allocation: each stays whole
     (export and predict equal the oracle's) while the others are freed in any
