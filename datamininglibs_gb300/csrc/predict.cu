@@ -409,12 +409,12 @@ dml_status dml_predict(const dml_forest* f, const float* samples, int64_t n_rows
     return DML_ERR_OOM;
   }
   dml_status st = DML_OK;
-  if (cudaMemcpyAsync(dX, samples, xb, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+  if (copy_host_device(dX, samples, xb, true, s) != cudaSuccess) {
     set_error("host to device copy failed");
     st = DML_ERR_CUDA;
   }
   if (st == DML_OK) st = predict_device(f, dX, n_rows, dout, s);
-  if (st == DML_OK && cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+  if (st == DML_OK && copy_host_device(out, dout, ob, false, s) != cudaSuccess) {
     set_error("device to host copy failed");
     st = DML_ERR_CUDA;
   }

@@ -171,8 +171,8 @@ def test_export_into_given_buffers(dml):
 
 def test_pinned_host_buffers_copied_by_sms(dml):
     """Samples and labels in pinned host memory are uploaded, and a model
-    exported into pinned buffers is downloaded, by SM copies through the
-    buffers' mapped pointers (the samples' and labels' sizes here, 156,052 and
+    exported into pinned buffers (and a prediction into a pinned result) is
+    downloaded, by SM copies through the buffers' mapped pointers (the samples' and labels' sizes here, 156,052 and
     12,004 bytes, leave a 4-byte tail for the copy engines): the same forest,
     bit for bit, as from and into pageable arrays."""
     torch = pytest.importorskip("torch")
@@ -188,6 +188,9 @@ def test_pinned_host_buffers_copied_by_sms(dml):
     pbuf = torch.empty(info.n_probs, dtype=torch.float32, pin_memory=True).numpy()
     nodes, probs = f.export(nbuf, pbuf)
     assert np.array_equal(nodes, rn) and np.array_equal(probs, rp)
+    # predict from pinned rows into a pinned result
+    out = torch.empty((X.shape[1], 5), dtype=torch.float32, pin_memory=True).numpy()
+    assert np.array_equal(f.predict(Xp, out=out), ref.predict(X))
 
 
 def test_forests_of_one_fit_free_independently(dml):
