@@ -157,8 +157,9 @@ cudaError_t copy_host_device(void* dst, const void* src, size_t bytes, bool to_d
   }
   const int4* from = (const int4*)(to_device ? mapped : src);
   int4* to = (int4*)(to_device ? dst : mapped);
-  int sms = 148;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  int sms = 148, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long n = (long long)(body / 16);
   const long long grid = std::min<long long>((long long)sms * 4, (n + 511) / 512);
   k_copy16<<<(unsigned)grid, 512, 0, s>>>(from, to, n);
@@ -555,8 +556,9 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       max_opt = std::max(max_opt, P.n_opt);
       if (P.algo == DML_ALGO_RF && P.N > tune.smem_cap) slot_stride = std::max(slot_stride, P.N);
     }
-    int sms = 148;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int sms = 148, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int big_grid = tune.big_ctas * sms;  // persistent CTAs
     if (slot_stride > 0) {
       // per-CTA scratch is 16 bytes per entry of the largest tree: at most 48 GB
