@@ -77,10 +77,12 @@ static __device__ __forceinline__ unsigned digit_excl_scan(unsigned tot, unsigne
   return ex;
 }
 
-// One LSD pass of pairs (kin, vin) -> (kout, vout) on byte `shift`, whose
-// digit histogram over all m keys is dh; a null vin stands for the values
-// 0 .. m-1.  Scratch written earlier in the same kernel is read with plain
+// One LSD pass of pairs (kin, vin) -> (kout, vout) on the 8-bit digit at bit
+// `shift`, whose histogram over all m keys is dh; a null vin stands for the
+// values 0 .. m-1.  Without VALS the keys move alone (packed keys carry their
+// values).  Scratch written earlier in the same kernel is read with plain
 // loads (never the read-only cache path).
+template <bool VALS>
 static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                                 uint32_t* vout, int m, int shift, const unsigned* dh,
                                 BigSmem& S) {
@@ -103,7 +105,7 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
     for (int r = 0; r < kBigPer; ++r) {
       const int i = wbeg + r * 32 + lane;
       k[r] = i < tn ? kin[base + i] : 0u;
-      v[r] = i < tn ? (vin ? vin[base + i] : (uint32_t)(base + i)) : 0u;
+      if (VALS) v[r] = i < tn ? (vin ? vin[base + i] : (uint32_t)(base + i)) : 0u;
     }
     for (int i = lane; i < 256; i += 32) S.whist[warp][i] = 0;
     __syncwarp();
@@ -152,7 +154,7 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
         const unsigned peers = pr[r];
         const unsigned pos = S.whist[warp][dgt] + __popc(peers & lt);
         S.tile[pos] = k[r];
-        S.tile[kBigTile + pos] = v[r];
+        if (VALS) S.tile[kBigTile + pos] = v[r];
         __syncwarp(mask);
         if ((peers & lt) == 0) S.whist[warp][dgt] += __popc(peers);
       }
@@ -164,7 +166,7 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
       const unsigned dgt = (kk >> shift) & 255u;
       const unsigned pos = S.running[cur][dgt] + (j - S.tstart[dgt]);
       kout[pos] = kk;
-      vout[pos] = S.tile[kBigTile + j];
+      if (VALS) vout[pos] = S.tile[kBigTile + j];
     }
     __syncthreads();
     cur ^= 1;
@@ -183,11 +185,29 @@ static __device__ bool big_sort(uint32_t* k, uint32_t* v, uint32_t* k2, uint32_t
     const int shift = 8 * d;
     if (((diff >> shift) & 255u) == 0) continue;
     if (primary)
-      big_pass(k, first ? v0 : v, k2, v2, m, shift, S.dh[d], S);
+      big_pass<true>(k, first ? v0 : v, k2, v2, m, shift, S.dh[d], S);
     else
-      big_pass(k2, v2, k, v, m, shift, S.dh[d], S);
+      big_pass<true>(k2, v2, k, v, m, shift, S.dh[d], S);
     primary = !primary;
     first = false;
+    __syncthreads();
+  }
+  return !primary;
+}
+
+// Sorts packed keys k (rank << pb | payload) of length m on their rank bits,
+// whose varying bits are `diff` (of the ranks) and whose digit histograms are
+// S.dh; returns true when the result is in k2, false when in k.
+static __device__ bool big_sort_keys(uint32_t* k, uint32_t* k2, int m, unsigned diff, int pb,
+                                     BigSmem& S) {
+  bool primary = true;
+  for (int d = 0; d < 4; ++d) {
+    if (((diff >> (8 * d)) & 255u) == 0) continue;
+    if (primary)
+      big_pass<false>(k, nullptr, k2, nullptr, m, pb + 8 * d, S.dh[d], S);
+    else
+      big_pass<false>(k2, nullptr, k, nullptr, m, pb + 8 * d, S.dh[d], S);
+    primary = !primary;
     __syncthreads();
   }
   return !primary;
@@ -213,6 +233,7 @@ struct BigArgs {
   uint32_t* pv;            // classification: label << 27 | weight per entry slot of the big nodes
   long long* pq;           // regression: packed (target, weight) per entry slot of the big nodes
   int* item_ctr;           // [phase - 1]: items handed out so far, zero before the launch
+  const int* maxw;         // the fit's largest entry weight
 };
 
 // Per-entry values of the big nodes, once per level instead of a gather by
@@ -435,11 +456,12 @@ __device__ __forceinline__ int col_of(int t) { return t + (t >> 5); }
 // an element changes, where the register form selects among the packed words
 // for every class on every element.  Results equal big_boundary<CW, INCR>.
 // cols: (C + 1) * kColStride words and C + 1 carries after them; nt: the
-// node's class counts (shared memory).  Two CTA barriers per tile.
-template <int CW>
+// node's class counts (shared memory).  Two CTA barriers per tile.  PK: the
+// keys are packed (rank << pb | label << wb | weight) and sv is not read.
+template <int CW, bool PK>
 static __device__ __noinline__ void big_boundary_cols(const uint32_t* sk, const uint32_t* sv,
                                                       int m, int per, const LNode& nd, int C,
-                                                      int ml,
+                                                      int ml, int pb, int wb,
                                                       const long long* H, long long prior,
                                                       const int* nt, uint32_t* cols,
                                                       float* out_g, int* out_p, long long* out_nl,
@@ -456,7 +478,8 @@ static __device__ __noinline__ void big_boundary_cols(const uint32_t* sk, const 
   for (int j = 0; j < CW; ++j) bL[j] = 0;
   for (int base = 0; base < m; base += kBigBlock * per) {
     const int p0 = base + tid * per;
-    const uint32_t prevk0 = p0 > 0 && p0 - 1 < m ? sk[p0 - 1] : 0u;
+    const uint32_t prevk0 =
+        p0 > 0 && p0 - 1 < m ? (PK ? sk[p0 - 1] >> pb : sk[p0 - 1]) : 0u;
     for (int c = 0; c <= C; ++c) cols[c * kColStride + me] = 0;
     uint32_t vq[kBigPer];
     unsigned bnd = 0;
@@ -468,8 +491,11 @@ static __device__ __noinline__ void big_boundary_cols(const uint32_t* sk, const 
         const int p = p0 + j;
         vq[j] = 0;
         if (j < per && p < m) {
-          const uint32_t kj = sk[p];
-          const uint32_t vv = sv[p];
+          const uint32_t raw = sk[p];
+          const uint32_t kj = PK ? raw >> pb : raw;
+          const uint32_t vv =
+              PK ? (((raw >> wb) & ((1u << (pb - wb)) - 1u)) << 27) | (raw & ((1u << wb) - 1u))
+                 : sv[p];
           vq[j] = vv;
           if (p > 0 && prev < kj) bnd |= 1u << j;
           prev = kj;
@@ -700,6 +726,18 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     const uint32_t* pv = b.pv ? b.pv + nd.ebeg : nullptr;
     const uint32_t* rk = P.rank ? P.rank + (long long)f * P.N : nullptr;
     const int nbytes = rk ? (32 - __clz(max(1ll, P.N - 1)) + 7) >> 3 : 4;
+    // packed keys (rank << pb | label << wb | weight) when the three fit one
+    // word: the sort then moves one word per entry instead of a key and a
+    // value, and the scan reads one
+    int wb = 0, pb = 0;
+    bool pk = false;
+    if constexpr (CW >= 2 && CW <= 5) {
+      if (packed && rk && pv) {
+        wb = 32 - __clz(max(1, *b.maxw));
+        pb = wb + (32 - __clz(max(1, P.C - 1)));
+        pk = (32 - __clz((int)max(1ll, P.N - 1))) + pb <= 32;
+      }
+    }
     for (int i = threadIdx.x; i < 4 * 256; i += kBigBlock) (&S.dh[0][0])[i] = 0;
     __syncthreads();
     unsigned o = 0, an = 0xFFFFFFFFu;
@@ -717,7 +755,12 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
         uint32_t k = 0;
         if (act) {
           k = rk ? __ldg(rk + rr[j]) : orderable(__ldg(xf + rr[j]));
-          k1[i] = k;
+          if (pk) {
+            const uint32_t pvi = __ldg(pv + i);
+            k1[i] = (k << pb) | ((pvi >> 27) << wb) | (pvi & 0x7FFFFFFu);
+          } else {
+            k1[i] = k;
+          }
           o |= k;
           an &= k;
         }
@@ -753,7 +796,9 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     // enter with the first pass; keys that are all equal need no pass and
     // have their values copied.
     bool in2 = false;
-    if (diff != 0) {
+    if (pk) {
+      if (diff != 0) in2 = big_sort_keys(k1, k2, m, diff, pb, S);
+    } else if (diff != 0) {
       in2 = big_sort(k1, v1, k2, v2, packed ? pv : nullptr, m, diff, S);
     } else {
       for (int i = threadIdx.x; i < m; i += kBigBlock) v1[i] = packed ? pv[i] : (uint32_t)i;
@@ -768,8 +813,12 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
     if (packed) {
       if constexpr (CW >= 2 && CW <= 5) {
         static_assert((2 * CW + 1) * (kColStride + 1) <= 2 * kBigTile, "columns fit the tiles");
-        big_boundary_cols<CW>(sk, sv, m, kBigPer, nd, P.C, max(1, P.min_leaf), a.H, s_prior,
-                              s_nt, S.tile, &g, &p, &nl, L);
+        if (pk)
+          big_boundary_cols<CW, true>(sk, sv, m, kBigPer, nd, P.C, max(1, P.min_leaf), pb, wb,
+                                      a.H, s_prior, s_nt, S.tile, &g, &p, &nl, L);
+        else
+          big_boundary_cols<CW, false>(sk, sv, m, kBigPer, nd, P.C, max(1, P.min_leaf), 0, 0,
+                                       a.H, s_prior, s_nt, S.tile, &g, &p, &nl, L);
       } else {
         big_boundary_items<CW>(sk, sv, m, nd, P, ncnt, a.H, s_prior, S.scan64, &g, &p, &nl, L);
       }
@@ -787,8 +836,10 @@ __global__ void __launch_bounds__(kBigBlock, big_ctas_per_sm(CW)) k_rf_big_items
       c.f = f;
       // the values on both sides of the boundary (-0 reads back as +0, which
       // gives the same threshold)
-      const float xa = packed ? key_value(P, f, sk[bp - 1]) : __ldg(xf + __ldg(rows + sv[bp - 1]));
-      const float xb = packed ? key_value(P, f, sk[bp]) : __ldg(xf + __ldg(rows + sv[bp]));
+      const uint32_t ka = pk ? sk[bp - 1] >> pb : sk[bp - 1];
+      const uint32_t kb = pk ? sk[bp] >> pb : sk[bp];
+      const float xa = packed ? key_value(P, f, ka) : __ldg(xf + __ldg(rows + sv[bp - 1]));
+      const float xb = packed ? key_value(P, f, kb) : __ldg(xf + __ldg(rows + sv[bp]));
       c.thr = midpoint_threshold(xa, xb);
       c.nl_e = bp;
       c.nl = (int)nl;
@@ -1008,8 +1059,8 @@ __global__ void __launch_bounds__(kBigBlock, smem_ctas_per_sm(CW)) k_rf_smem(Lev
       if constexpr (CW >= 2 && CW <= 5) cols_scan = (C + 1) * (kColStride + 1) <= 2 * cap;
       if (packed && cols_scan) {
         // the class columns in the sort buffers the sorted pairs are not in
-        big_boundary_cols<CW>(sk, sv, m, per, nd, C, max(1, P.min_leaf), a.H, s_prior, s_nt,
-                              in2 ? k1 : k2, &g, &p, &nl, L);
+        big_boundary_cols<CW, false>(sk, sv, m, per, nd, C, max(1, P.min_leaf), 0, 0, a.H,
+                                     s_prior, s_nt, in2 ? k1 : k2, &g, &p, &nl, L);
       } else if (packed) {
         big_boundary<CW, false>(sk, sv, m, per, nd, P, ncnt, a.H, s_prior, scan64, &g, &p, &nl, L);
       } else {

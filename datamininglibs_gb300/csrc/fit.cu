@@ -581,6 +581,8 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
         slot_stride > 0 && any_reg ? (long long*)alloc(sizeof(long long) * total_slots) : nullptr;
     // [0] retry count of the big-node search, [1..2] its item counters per phase
     int* d_nretry = (int*)alloc(sizeof(int) * 3);
+    // the largest entry weight (0 without bootstrap weights: read as 1)
+    int* d_maxw = (int*)alloc(sizeof(int));
     ProbDesc* d_probs = (ProbDesc*)alloc(sizeof(ProbDesc) * nprob);
     DML_CK(cudaMemcpyAsync(d_probs, hp.data(), sizeof(ProbDesc) * nprob, cudaMemcpyHostToDevice, s));
     std::vector<int> tree_prob(total_trees);
@@ -635,6 +637,17 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
       k_boot_count<<<g, 256, 0, s>>>(d_probs, d_tree_prob, boot, chunk);
       DML_CK(cudaGetLastError());
       ++st.launches;
+    }
+    {
+      DML_CK(cudaMemsetAsync(d_maxw, 0, sizeof(int), s));  // read as at least 1
+      if (any_weights) {
+        int sms = 148, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        k_max_weight<<<sms * 4, 256, 0, s>>>(boot, total_slots, d_maxw);
+        DML_CK(cudaGetLastError());
+        ++st.launches;
+      }
     }
     k_roots<1024><<<total_trees, 1024, 0, s>>>(d_probs, d_tree_prob, boot, rowsA,
                                                wA, cur.p, cnt_cur.p, Cmax, res_cur.p, queues(),
@@ -741,6 +754,7 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
           b.pv = big_pv;
           b.pq = big_pq;
           b.item_ctr = d_nretry + 1;
+          b.maxw = d_maxw;
           b.L.stats = d_stats + 4 + 4 * q;
           DML_CK(cudaEventRecord(qev[q][0], sq));
           const int chunk = plain ? kPlainChunk : nb;

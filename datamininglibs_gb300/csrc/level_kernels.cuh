@@ -807,6 +807,18 @@ __global__ void k_to_pnodes(const ClassifyNode* nodes, long long n, const float*
   }
 }
 
+// The largest bootstrap multiplicity of the fit, for the big-node items'
+// packed sort keys (rank, label and weight in one word).
+__global__ void k_max_weight(const int* __restrict__ w, long long n, int* out) {
+  int mx = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    mx = max(mx, w[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(out, mx);
+}
+
 // Compact predict layout (PNode8) from the 16-byte one; *bad is set when a
 // child offset does not fit the bits above the feature field.
 __global__ void k_to_pnodes8(const PNode* in, long long n, int fbits, PNode8* out, int* bad) {
