@@ -24,6 +24,7 @@ constexpr int kBigBlock = 256;
 constexpr int kBigPer = 8;                       // elements per thread
 constexpr int kBigTile = kBigBlock * kBigPer;    // 2048
 constexpr int kBigWarps = kBigBlock / 32;
+constexpr int kBigPerKeys = 16;                  // elements per thread of a keys-only pass
 
 struct BigSmem {
   unsigned whist[kBigWarps][256];
@@ -80,13 +81,16 @@ static __device__ __forceinline__ unsigned digit_excl_scan(unsigned tot, unsigne
 // One LSD pass of pairs (kin, vin) -> (kout, vout) on the 8-bit digit at bit
 // `shift`, whose histogram over all m keys is dh; a null vin stands for the
 // values 0 .. m-1.  Without VALS the keys move alone (packed keys carry their
-// values).  Scratch written earlier in the same kernel is read with plain
-// loads (never the read-only cache path).
-template <bool VALS>
+// values, and PER elements a thread fill the whole tile buffer).  Scratch
+// written earlier in the same kernel is read with plain loads (never the
+// read-only cache path).
+template <bool VALS, int PER = kBigPer>
 static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                                 uint32_t* vout, int m, int shift, const unsigned* dh,
                                 BigSmem& S) {
   static_assert(kBigBlock == 256, "one thread per digit");
+  constexpr int T = kBigBlock * PER;  // entries a tile
+  static_assert(VALS ? T == kBigTile : T <= 2 * kBigTile, "the tile fits its buffer");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int dg = threadIdx.x;
   const unsigned lt = (1u << lane) - 1u;
@@ -97,21 +101,21 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
   // running positions are double-buffered (tile t reads running[cur] and
   // writes running[cur ^ 1] for tile t + 1)
   int cur = 0;
-  for (int base = 0; base < m; base += kBigTile) {
-    const int tn = min(kBigTile, m - base);
-    const int wbeg = warp * 256;
-    uint32_t k[kBigPer], v[kBigPer];
+  for (int base = 0; base < m; base += T) {
+    const int tn = min(T, m - base);
+    const int wbeg = warp * 32 * PER;
+    uint32_t k[PER], v[VALS ? PER : 1];
 #pragma unroll
-    for (int r = 0; r < kBigPer; ++r) {
+    for (int r = 0; r < PER; ++r) {
       const int i = wbeg + r * 32 + lane;
       k[r] = i < tn ? kin[base + i] : 0u;
       if (VALS) v[r] = i < tn ? (vin ? vin[base + i] : (uint32_t)(base + i)) : 0u;
     }
     for (int i = lane; i < 256; i += 32) S.whist[warp][i] = 0;
     __syncwarp();
-    unsigned pr[kBigPer];  // each element's equal-digit lanes, reused by the scatter
+    unsigned pr[PER];  // each element's equal-digit lanes, reused by the scatter
 #pragma unroll
-    for (int r = 0; r < kBigPer; ++r) {
+    for (int r = 0; r < PER; ++r) {
       const int i = wbeg + r * 32 + lane;
       const bool act = i < tn;
       const unsigned mask = __ballot_sync(kFull, act);
@@ -145,7 +149,7 @@ static __device__ void big_pass(const uint32_t* kin, const uint32_t* vin, uint32
     }
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < kBigPer; ++r) {
+    for (int r = 0; r < PER; ++r) {
       const int i = wbeg + r * 32 + lane;
       const bool act = i < tn;
       const unsigned mask = __ballot_sync(kFull, act);
@@ -204,9 +208,9 @@ static __device__ bool big_sort_keys(uint32_t* k, uint32_t* k2, int m, unsigned 
   for (int d = 0; d < 4; ++d) {
     if (((diff >> (8 * d)) & 255u) == 0) continue;
     if (primary)
-      big_pass<false>(k, nullptr, k2, nullptr, m, pb + 8 * d, S.dh[d], S);
+      big_pass<false, kBigPerKeys>(k, nullptr, k2, nullptr, m, pb + 8 * d, S.dh[d], S);
     else
-      big_pass<false>(k2, nullptr, k, nullptr, m, pb + 8 * d, S.dh[d], S);
+      big_pass<false, kBigPerKeys>(k2, nullptr, k, nullptr, m, pb + 8 * d, S.dh[d], S);
     primary = !primary;
     __syncthreads();
   }
