@@ -127,13 +127,9 @@ void dev_free(void* p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
 }
 
-// Keeps freed pool memory cached in this process so that repeated fits and
-// predictions reuse device buffers instead of returning to the driver.  The
-// release threshold is an attribute of each device's own pool, so it is set
-// once per device (the first fit on it).
-// Host <-> device copies of pinned buffers by SMs.  On the GB300 machines the
-// copy engines' rate between pinned host memory and the device has varied
-// over time (other jobs share the host); in one probe it fell from 193-211 to
+// Host <-> device copies of pinned buffers by SMs.  On GB300 hosts shared
+// with other jobs the copy engines' rate between pinned host memory and the
+// device has varied over time; in one probe it fell from 193-211 to
 // 26-54 GB/s while SM copies through the same buffers' mapped pointers still
 // ran at 104-193 GB/s, and on an unloaded link both ran at 193-210 GB/s.
 __global__ void k_copy16(const int4* __restrict__ src, int4* __restrict__ dst, long long n) {
@@ -149,9 +145,20 @@ cudaError_t copy_host_device(void* dst, const void* src, size_t bytes, bool to_d
   void* mapped = nullptr;
   const size_t body = bytes & ~(size_t)15;
   const bool aligned = ((uintptr_t)dst % 16 == 0) && ((uintptr_t)src % 16 == 0);
-  if (body == 0 || !aligned ||
+  // Where the GPU reaches pageable memory through the host's page tables
+  // (Grace), cudaHostGetDevicePointer maps pageable memory too.  SM loads from
+  // it are fast (a 102 MB predict input: 3.5 ms against 8.8 ms by
+  // cudaMemcpyAsync), but SM stores into pages not yet touched fault them in
+  // one by one (a 433 MB export into fresh arrays: 117 ms against 16 ms), so
+  // device-to-host copies take SMs only into page-locked memory
+  // (cudaHostAlloc / cudaHostRegister).  The callers synchronise before they
+  // return, so pageable sources are read before the caller can reuse them.
+  cudaPointerAttributes at{};
+  const bool locked = cudaPointerGetAttributes(&at, host) == cudaSuccess &&
+                      at.type == cudaMemoryTypeHost;
+  if (body == 0 || !aligned || (!to_device && !locked) ||
       cudaHostGetDevicePointer(&mapped, const_cast<void*>(host), 0) != cudaSuccess) {
-    cudaGetLastError();  // not pinned (or not mapped): the copy engines
+    cudaGetLastError();  // pageable destination (or not mapped): the copy engines
     return cudaMemcpyAsync(dst, src, bytes,
                            to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s);
   }
@@ -169,6 +176,10 @@ cudaError_t copy_host_device(void* dst, const void* src, size_t bytes, bool to_d
                          to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s);
 }
 
+// Keeps freed pool memory cached in this process so that repeated fits and
+// predictions reuse device buffers instead of returning to the driver.  The
+// release threshold is an attribute of each device's own pool, so it is set
+// once per device (the first fit on it).
 void init_pool_once() {
   constexpr int kMaxDev = 64;
   static std::once_flag once[kMaxDev];
