@@ -68,8 +68,8 @@ int quant_scale_from_max(float maxabs, long long n);
 dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s);
 // Copies `bytes` between a host buffer and device memory on stream s: with
 // SM loads and stores through the host buffer's mapped device pointer when both
-// ends are 16-byte aligned and the buffer is mapped (a device-to-host copy only
-// into page-locked memory), else by cudaMemcpyAsync.
+// ends are 16-byte aligned and the buffer is mapped (a device-to-host copy of
+// 16 MB or more only into page-locked memory), else by cudaMemcpyAsync.
 cudaError_t copy_host_device(void* dst, const void* src, size_t bytes, bool to_device,
                              cudaStream_t s);
 void forest_build_pnodes8(const dml_forest* f, cudaStream_t s);

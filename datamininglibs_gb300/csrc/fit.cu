@@ -147,18 +147,24 @@ cudaError_t copy_host_device(void* dst, const void* src, size_t bytes, bool to_d
   const bool aligned = ((uintptr_t)dst % 16 == 0) && ((uintptr_t)src % 16 == 0);
   // Where the GPU reaches pageable memory through the host's page tables
   // (Grace), cudaHostGetDevicePointer maps pageable memory too.  SM loads from
-  // it are fast (a 102 MB predict input: 3.5 ms against 8.8 ms by
-  // cudaMemcpyAsync), but SM stores into pages not yet touched fault them in
-  // one by one (a 433 MB export into fresh arrays: 117 ms against 16 ms), so
-  // device-to-host copies take SMs only into page-locked memory
-  // (cudaHostAlloc / cudaHostRegister).  The callers synchronise before they
-  // return, so pageable sources are read before the caller can reuse them.
-  cudaPointerAttributes at{};
-  const bool locked = cudaPointerGetAttributes(&at, host) == cudaSuccess &&
-                      at.type == cudaMemoryTypeHost;
-  if (body == 0 || !aligned || (!to_device && !locked) ||
-      cudaHostGetDevicePointer(&mapped, const_cast<void*>(host), 0) != cudaSuccess) {
-    cudaGetLastError();  // pageable destination (or not mapped): the copy engines
+  // it are fast.  SM stores into pages not yet touched fault them in one by
+  // one, about 0.28 ms per MB (a 433 MB export into fresh arrays: 117-130 ms),
+  // while cudaMemcpyAsync into fresh pageable memory costs a few milliseconds
+  // per call plus about 0.03 ms per MB (16-18 ms for the same export, 7-9 ms
+  // for an 8 MB predict output that SMs wrote in about 2.3 ms).  So copies to
+  // the host take SMs into page-locked memory (cudaHostAlloc /
+  // cudaHostRegister) and into pageable memory below kSmPageableStore bytes.
+  // The callers synchronise before they return, so pageable sources are read
+  // before the caller can reuse them.
+  constexpr size_t kSmPageableStore = 16u << 20;
+  bool sm = body != 0 && aligned &&
+            cudaHostGetDevicePointer(&mapped, const_cast<void*>(host), 0) == cudaSuccess;
+  if (sm && !to_device && bytes >= kSmPageableStore) {
+    cudaPointerAttributes at{};
+    sm = cudaPointerGetAttributes(&at, host) == cudaSuccess && at.type == cudaMemoryTypeHost;
+  }
+  if (!sm) {
+    cudaGetLastError();  // not mapped, or a pageable destination: the copy engines
     return cudaMemcpyAsync(dst, src, bytes,
                            to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s);
   }
