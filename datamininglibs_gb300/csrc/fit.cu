@@ -1044,6 +1044,10 @@ static std::vector<dml_forest*> run_fit(const dml_fit_desc* descs, int nprob, bo
     DML_CK(cudaStreamSynchronize(s));
     finish_stats(st);
   } catch (...) {
+    // a failure in the middle of a level can leave kernels queued on the
+    // node classes' own streams, which are joined to s only after all of a
+    // level's launches: wait for the whole device before the buffers go
+    cudaDeviceSynchronize();
     for (dml_forest* f : forests) dml_forest_free(f);
     release_all();
     cudaStreamSynchronize(s);
