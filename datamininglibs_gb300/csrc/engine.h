@@ -28,10 +28,13 @@ struct dml_forest {
   long long n_probs = 0;
   dml::PNode* pnodes = nullptr;        // device, predict layout
   // device, compact predict layout (null when it does not fit or before the
-  // first bulk prediction, which builds it) and its feature bits
+  // first bulk prediction, which builds it) and its feature bits.  p8_ready is
+  // set (release) once both are final and the layout's kernel has completed;
+  // a reader that sees it false builds under p8_mu, which waits for a build
+  // another thread has started.
   mutable dml::PNode8* pnodes8 = nullptr;
   mutable int p8_bits = 0;
-  mutable bool p8_tried = false;
+  mutable std::atomic<bool> p8_ready{false};
   mutable std::mutex p8_mu;
   float* gains = nullptr;              // device, FP32 gain per node (NaN for leaves); null
                                        // for forests not fitted by this engine

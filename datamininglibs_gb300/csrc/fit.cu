@@ -1081,8 +1081,7 @@ dml_status forest_build_pnodes(dml_forest* f, cudaStream_t s) {
 // prediction walks the 16-byte one).  Synchronises s.
 void forest_build_pnodes8(const dml_forest* f, cudaStream_t s) {
   std::lock_guard<std::mutex> lock(f->p8_mu);
-  if (f->p8_tried) return;
-  f->p8_tried = true;
+  if (f->p8_ready.load(std::memory_order_acquire)) return;
   const int g = (int)std::min<long long>(8192, (f->n_nodes + 255) / 256 + 1);
   int fb = 1;
   while ((1 << fb) - 1 < f->n_features) ++fb;
@@ -1108,6 +1107,7 @@ void forest_build_pnodes8(const dml_forest* f, cudaStream_t s) {
     cudaGetLastError();
     f->pnodes8 = nullptr;
   }
+  f->p8_ready.store(true, std::memory_order_release);
 }
 
 static dml_status fit_entry(const dml_fit_desc* descs, int n, dml_forest** out, void* stream,

@@ -326,7 +326,7 @@ dml_status predict_device(const dml_forest* f, const float* dX, long long n_rows
   // DML_PREDICT_NODE16 is set
   const char* n16 = getenv("DML_PREDICT_NODE16");
   const bool compact = n_rows >= kPassMinRows && !(n16 && atoi(n16) != 0);
-  if (compact && !f->p8_tried) forest_build_pnodes8(f, s);
+  if (compact && !f->p8_ready.load(std::memory_order_acquire)) forest_build_pnodes8(f, s);
   const bool use8 = compact && f->pnodes8 != nullptr;
   const int per = n_rows >= kPassMinRows
                       ? predict_pass_trees(f, use8 ? (long long)sizeof(PNode8) : (long long)sizeof(PNode))
